@@ -1,0 +1,323 @@
+#!/usr/bin/env python3
+"""Benchmark of the particle-mesh step on the 20M-particle / 2048^2 CIC disk.
+
+One step = deposit -> FFT convolution -> force -> gather + update over all
+20,000,000 particles (the drop-in headline workload: exponential disk of scale
+length 200 cells at the lattice centre, circular velocities from the enclosed
+mass plus 5% dispersion, lognormal(0, 0.3) masses, dt = 0.001).  Inputs are
+seeded synthetic data of that shape.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line.  `value` is device-timed throughput (particle-steps/s)
+with the state resident in HBM; `e2e` is the same metric through the C ABI
+with host buffers: the state uploaded from page-locked host memory inside the
+timed region and the positions read back to page-locked host memory after
+every step.  --impl reference times the reference algorithm on the host
+cores (the CPU restatement of CosmosCuda.cuh's step; the reference itself has
+no CPU step).  With N > 1 (torchrun) every rank runs an independent replica
+(the step is not sharded across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @20M, 2048²: plain FP32 vs TC split-FFT at ≤1e-5 rel force err"
+UNIT = "particle-steps/s"
+WORKLOAD = "disk-20M-2048-cic"
+
+
+# ---- small cudart helper (events on the library's stream, pinned memory) ----------------
+class CudaRT:
+    def __init__(self):
+        self.lib = None
+        for name in ("libcudart.so.13", "libcudart.so", "libcudart.so.12"):
+            try:
+                self.lib = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        if self.lib is None:
+            raise RuntimeError("libcudart not found")
+        L = self.lib
+        L.cudaEventCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+        L.cudaEventRecord.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
+        L.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
+        L.cudaEventDestroy.argtypes = [ctypes.c_void_p]
+        L.cudaHostRegister.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint]
+        L.cudaHostUnregister.argtypes = [ctypes.c_void_p]
+        L.cudaSetDevice.argtypes = [ctypes.c_int]
+        L.cudaMalloc.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
+        L.cudaFree.argtypes = [ctypes.c_void_p]
+        L.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+
+    def event(self):
+        e = ctypes.c_void_p()
+        assert self.lib.cudaEventCreate(ctypes.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        assert self.lib.cudaEventRecord(e, ctypes.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b):
+        assert self.lib.cudaEventSynchronize(b) == 0
+        t = ctypes.c_float()
+        assert self.lib.cudaEventElapsedTime(ctypes.byref(t), a, b) == 0
+        return t.value
+
+    def pin(self, arr):
+        rc = self.lib.cudaHostRegister(ctypes.c_void_p(arr.ctypes.data), arr.nbytes, 0)
+        if rc != 0:
+            raise RuntimeError(f"cudaHostRegister failed ({rc})")
+
+    def unpin(self, arr):
+        self.lib.cudaHostUnregister(ctypes.c_void_p(arr.ctypes.data))
+
+
+# ---- clocks sampled during the timed region ----------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ---- CPU baseline: the reference algorithm restated on the host cores ---------------------
+def cpu_baseline(state, N, cic, dt, budget_s: float, min_steps: int = 2):
+    from oracle import pm_oracle
+    threads = os.cpu_count() or 1
+    pm_oracle.set_threads(threads)
+    o = pm_oracle.OraclePM(N, cic, dt, 1.0, fp64=False)
+    s = state.copy()
+    o.step(s.x, s.y, s.x_old, s.y_old, s.m, 1)  # warm-up (page-in, thread pool)
+    n = 0
+    t0 = time.perf_counter()
+    while n < min_steps or (time.perf_counter() - t0) < budget_s:
+        o.step(s.x, s.y, s.x_old, s.y_old, s.m, 1)
+        n += 1
+    dt_s = time.perf_counter() - t0
+    o.close()
+    return {"value": state.count * n / dt_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} full steps of the {state.count}-particle {N}^2 {'CIC' if cic else 'NGP'} workload "
+                      f"(FP32 restatement of the reference step, OpenMP over {threads} threads)"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--particles", type=int, default=None, help="override the particle count (testing)")
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sort-interval", type=int, default=-1)
+    args = ap.parse_args()
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    from cosmossimulationwithcuda_gb300 import ics
+
+    w = ics.WORKLOADS[WORKLOAD]
+    N, cic, dt = w["N"], w["cic"], w["dt"]
+    P = args.particles or w["P"]
+    state = ics.make_workload(WORKLOAD, P)
+    config = {"workload": WORKLOAD, "particles": P, "lattice": N, "deposit": "CIC" if cic else "NGP", "dt": dt,
+              "ic": "exponential disk, scale 200 cells, v_c from enclosed mass + 5% dispersion, lognormal(0,0.3) masses",
+              "l2": "particle state (20 B/particle = 400 MB) exceeds the 126 MB L2 every step; the lattice "
+                    "fields (~70 MB) stay L2-resident by design"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(state, N, cic, dt, args.cpu_budget)
+        # the reference arm: each "step" is a bounded sample of the workload on the host cores
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": P / cb["value"] * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded)", "config": config, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    from cosmossimulationwithcuda_gb300 import _build, _lib
+    _build.build()
+    rt = CudaRT()
+    rt.lib.cudaSetDevice(local)
+    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=args.sort_interval)
+    stream = sim.stream()
+    sim.set_state(state)
+
+    # ---- device-timed throughput (state resident) ----
+    sim.step(args.warmup)
+    sim.synchronize()
+    e0, e1 = rt.event(), rt.event()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        rt.record(e0, stream)
+        sim.step(args.steps)
+        rt.record(e1, stream)
+        ms = rt.elapsed_ms(e0, e1)
+    sim.synchronize()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = P * args.steps * ws / (ms / 1e3)
+
+    # ---- per-stage times (profiled direct launches, events between kernels) ----
+    sim.set_profiling(True)
+    prof_steps = 20
+    acc = np.zeros(7)
+    for _ in range(prof_steps):
+        sim.step(1)
+        acc += np.pad(sim.stage_times(), (0, 7))[:7]
+    sim.set_profiling(False)
+    sim.synchronize()
+    stage_ms = acc / prof_steps
+    names = ["deposit", "fft_conv", "-", "-", "force", "integrate", "sort"]
+    stages = {n: round(float(t), 5) for n, t in zip(names, stage_ms) if n != "-"}
+    # dominant kernel and its algorithmic bytes per launch
+    algo = {"deposit": 12.0 * P + 4.0 * N * N, "integrate": 32.0 * P + 8.0 * N * N,
+            "fft_conv": 25.0 * N * N, "force": 12.0 * N * N}
+    dom = max(algo, key=lambda k: stages.get(k, 0.0))
+    peak, peak_kind = measured_peak_gbs()
+    achieved = algo[dom] / (stages[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": algo[dom], "traffic": None}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    try:
+        hx = np.empty(P, np.float32)
+        hy = np.empty(P, np.float32)
+        host_state = state.copy()
+        pinned = [hx, hy, host_state.x, host_state.y, host_state.x_old, host_state.y_old, host_state.m]
+        for a in pinned:
+            rt.pin(a)
+        sim.synchronize()
+        e2e_steps = args.steps
+        t0 = time.perf_counter()
+        sim.set_state(host_state)
+        tickets = []
+        for _ in range(e2e_steps):
+            sim.step(1)
+            tickets.append(sim.positions_async(hx, hy, ordered=False))
+        sim.wait(tickets[-1])
+        sim.synchronize()
+        t1 = time.perf_counter()
+        for a in pinned:
+            rt.unpin(a)
+        e2e = {"value": P * e2e_steps / (t1 - t0), "unit": UNIT,
+               "h2d_bytes_per_step": int(20 * P / e2e_steps), "d2h_bytes_per_step": int(8 * P),
+               "note": "state uploaded once from page-locked memory (bytes amortised over the steps); "
+                       "x, y read back after every step"}
+    except Exception as exc:  # report, never hide
+        e2e = {"value": None, "unit": UNIT, "error": str(exc)}
+
+    launches = sim.launches_per_step() * args.steps
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(state, N, cic, dt, args.cpu_budget)
+    sim.close()
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
+            "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": launches, "stages_ms": stages}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

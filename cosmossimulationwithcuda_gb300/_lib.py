@@ -1,0 +1,255 @@
+"""ctypes binding of the cosmos_pm C ABI (include/cosmos_pm.h).
+
+The CUDA library is built in-tree (cosmossimulationwithcuda_gb300/libcosmos_pm.so,
+see build.py).  Loading fails loudly when it is missing: there is no CPU
+fallback for any part of the step.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcosmos_pm.so")
+
+COSMOS_OK = 0
+ERRORS = {-1: "INVALID", -2: "CUDA", -3: "NOMEM", -4: "RANGE", -5: "TIMEOUT", -6: "STATE"}
+DEPOSIT_NGP, DEPOSIT_CIC = 0, 1
+FORCE_GRADIENT, FORCE_SPECTRAL = 0, 1
+FIELD_DENSITY, FIELD_POTENTIAL, FIELD_FORCE = 0, 1, 2
+STAGE_DEPOSIT, STAGE_POTENTIAL, STAGE_FORCE, STAGE_INTEGRATE = 0, 1, 2, 3
+
+# Every function include/cosmos_pm.h declares (checked by the CPU test suite).
+EXPORTS = (
+    "cosmos_pm_default_config", "cosmos_pm_create", "cosmos_pm_destroy", "cosmos_pm_set_particles",
+    "cosmos_pm_get_particles", "cosmos_pm_clear", "cosmos_pm_step", "cosmos_pm_synchronize",
+    "cosmos_pm_get_positions_async", "cosmos_pm_poll", "cosmos_pm_wait", "cosmos_pm_run_stage",
+    "cosmos_pm_get_field", "cosmos_pm_set_field", "cosmos_pm_sort", "cosmos_pm_tile_keys",
+    "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
+    "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
+)
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("lattice_n", ctypes.c_int32),
+        ("deposit", ctypes.c_int32),
+        ("dt", ctypes.c_float),
+        ("gravity_multiplier", ctypes.c_float),
+        ("num_particles", ctypes.c_int64),
+        ("device", ctypes.c_int32),
+        ("force_mode", ctypes.c_int32),
+        ("sort_interval", ctypes.c_int32),
+        ("sort_granularity", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
+    ]
+
+
+class CosmosError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cosmos_pm error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+_lib = None
+_f32p = ctypes.POINTER(ctypes.c_float)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+
+
+def load(path: str | None = None):
+    """Load libcosmos_pm.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"cosmos_pm CUDA library not built ({path}); run build() first")
+    L = ctypes.CDLL(path)
+    i32, i64 = ctypes.c_int32, ctypes.c_int64
+    sig = {
+        "cosmos_pm_default_config": (None, [ctypes.POINTER(Config)]),
+        "cosmos_pm_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(_vp)]),
+        "cosmos_pm_destroy": (ctypes.c_int, [_vp]),
+        "cosmos_pm_set_particles": (ctypes.c_int, [_vp, _f32p, _f32p, _f32p, _f32p, _f32p, i64, i64]),
+        "cosmos_pm_get_particles": (ctypes.c_int, [_vp, _f32p, _f32p, _f32p, _f32p, _f32p, i64, i64]),
+        "cosmos_pm_clear": (ctypes.c_int, [_vp]),
+        "cosmos_pm_step": (ctypes.c_int, [_vp, i32]),
+        "cosmos_pm_synchronize": (ctypes.c_int, [_vp]),
+        "cosmos_pm_get_positions_async": (ctypes.c_int, [_vp, _f32p, _f32p, i32, ctypes.POINTER(ctypes.c_uint64)]),
+        "cosmos_pm_poll": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.POINTER(i32)]),
+        "cosmos_pm_wait": (ctypes.c_int, [_vp, ctypes.c_uint64]),
+        "cosmos_pm_run_stage": (ctypes.c_int, [_vp, i32]),
+        "cosmos_pm_get_field": (ctypes.c_int, [_vp, i32, _f32p]),
+        "cosmos_pm_set_field": (ctypes.c_int, [_vp, i32, _f32p]),
+        "cosmos_pm_sort": (ctypes.c_int, [_vp, _u32p]),
+        "cosmos_pm_tile_keys": (ctypes.c_int, [_vp, _f32p, _f32p, i64, i32, _u32p]),
+        "cosmos_pm_diagnostics": (ctypes.c_int, [_vp, _f64p, _f64p, _f64p, _f64p]),
+        "cosmos_pm_set_profiling": (ctypes.c_int, [_vp, i32]),
+        "cosmos_pm_stage_times": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(i32)]),
+        "cosmos_pm_stream": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64)]),
+        "cosmos_pm_launches_per_step": (ctypes.c_int, [_vp, ctypes.POINTER(i32)]),
+        "cosmos_pm_last_error": (ctypes.c_char_p, [_vp]),
+        "cosmos_pm_version": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a, ctype=_f32p):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctype)
+
+
+def default_config(**kw) -> Config:
+    c = Config()
+    load().cosmos_pm_default_config(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Simulation:
+    """One particle-mesh simulation on one GPU, driven through the C ABI.
+
+    Mirrors the reference Universe<K> (CosmosCuda.cuh:830-1428): construction
+    builds the filter, set_particles uploads state (constructor / addGalaxy
+    uploads), clear() parks every particle, step() enqueues steps."""
+
+    def __init__(self, N: int, P: int, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0,
+                 device: int = 0, force_mode: int = FORCE_GRADIENT, sort_interval: int = -1,
+                 sort_granularity: int = -1, use_graph: bool = True):
+        self.L = load()
+        self.cfg = default_config(lattice_n=N, deposit=DEPOSIT_CIC if cic else DEPOSIT_NGP, dt=dt,
+                                  gravity_multiplier=gravity_multiplier, num_particles=P, device=device,
+                                  force_mode=force_mode, sort_interval=sort_interval,
+                                  sort_granularity=sort_granularity, use_graph=int(use_graph))
+        h = _vp()
+        rc = self.L.cosmos_pm_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if rc != COSMOS_OK:
+            raise CosmosError(rc, self.L.cosmos_pm_last_error(None).decode())
+        self.h = h
+        self.N, self.P, self.cic, self.dt = N, P, cic, dt
+
+    # -- lifetime -------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cosmos_pm_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != COSMOS_OK:
+            raise CosmosError(rc, self.L.cosmos_pm_last_error(self.h).decode())
+
+    # -- particle state -------------------------------------------------------
+    def set_particles(self, x, y, x_old=None, y_old=None, m=None, offset: int = 0):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (x, y, x_old, y_old, m)]
+        n = arrs[0].size
+        self._check(self.L.cosmos_pm_set_particles(self.h, *[_ptr(a) for a in arrs], n, offset))
+
+    def set_state(self, s):
+        self.set_particles(s.x, s.y, s.x_old, s.y_old, s.m)
+
+    def get_particles(self, count: int | None = None, offset: int = 0):
+        count = self.P - offset if count is None else count
+        out = [np.empty(count, np.float32) for _ in range(5)]
+        self._check(self.L.cosmos_pm_get_particles(self.h, *[_ptr(a) for a in out], count, offset))
+        return out
+
+    def clear(self):
+        self._check(self.L.cosmos_pm_clear(self.h))
+
+    # -- stepping -------------------------------------------------------------
+    def step(self, n: int = 1):
+        self._check(self.L.cosmos_pm_step(self.h, n))
+
+    def synchronize(self):
+        self._check(self.L.cosmos_pm_synchronize(self.h))
+
+    def positions_async(self, hx, hy, ordered: bool = True) -> int:
+        t = ctypes.c_uint64()
+        self._check(self.L.cosmos_pm_get_positions_async(self.h, _ptr(hx), _ptr(hy), int(ordered), ctypes.byref(t)))
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = ctypes.c_int32()
+        self._check(self.L.cosmos_pm_poll(self.h, ticket, ctypes.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket: int):
+        self._check(self.L.cosmos_pm_wait(self.h, ticket))
+
+    # -- stages and fields ----------------------------------------------------
+    def run_stage(self, stage: int):
+        self._check(self.L.cosmos_pm_run_stage(self.h, stage))
+
+    def get_field(self, field: int):
+        shape = (self.N, self.N, 2) if field == FIELD_FORCE else (self.N, self.N)
+        out = np.empty(shape, np.float32)
+        self._check(self.L.cosmos_pm_get_field(self.h, field, _ptr(out)))
+        return out
+
+    def set_field(self, field: int, a):
+        a = np.ascontiguousarray(a, np.float32)
+        self._check(self.L.cosmos_pm_set_field(self.h, field, _ptr(a)))
+
+    def sort(self):
+        perm = np.empty(self.P, np.uint32)
+        self._check(self.L.cosmos_pm_sort(self.h, _ptr(perm, _u32p)))
+        return perm
+
+    def tile_keys(self, x, y, granularity: int):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        keys = np.empty(x.size, np.uint32)
+        self._check(self.L.cosmos_pm_tile_keys(self.h, _ptr(x), _ptr(y), x.size, granularity, _ptr(keys, _u32p)))
+        return keys
+
+    def diagnostics(self):
+        v = [ctypes.c_double() for _ in range(4)]
+        self._check(self.L.cosmos_pm_diagnostics(self.h, *[ctypes.byref(a) for a in v]))
+        return tuple(a.value for a in v)
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.cosmos_pm_set_profiling(self.h, int(on)))
+
+    def stage_times(self):
+        t = np.zeros(8, np.float32)
+        n = ctypes.c_int32(8)
+        self._check(self.L.cosmos_pm_stage_times(self.h, _ptr(t), ctypes.byref(n)))
+        return t[: n.value]
+
+    def stream(self) -> int:
+        s = ctypes.c_uint64()
+        self._check(self.L.cosmos_pm_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int32()
+        self._check(self.L.cosmos_pm_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+
+def version() -> str:
+    return load().cosmos_pm_version().decode()

@@ -1,0 +1,763 @@
+// C ABI of the cosmos_pm library: handle lifetime, particle I/O, the step
+// sequence (direct launches or a replayed CUDA graph), asynchronous position
+// readback, stage-level test hooks and diagnostics.
+//
+// Stands in for the Universe<K> class of CosmosCuda.cuh (constructor
+// :881-1035, clear :1038-1069, step methods :1209-1300, worker loop
+// :1318-1364, destructor :1396-1427).  The reference's multi-GPU exchange,
+// render chain and frame ring are not part of this path.
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pm_common.cuh"
+#include "pm_internal.h"
+
+namespace cpm {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+const char* last_error_message() { return g_last_error.c_str(); }
+
+}  // namespace cpm
+
+using cpm::ParticleArrays;
+
+enum StageIdx { kStDeposit = 0, kStRows, kStCols, kStRowsInv, kStForce, kStIntegrate, kStSort, kNumStages };
+
+struct cosmos_pm {
+    cosmos_pm_config cfg{};
+    int N = 0, logN = 0, cic = 0, nsm = 0, device = 0;
+    int64_t P = 0, Pq = 0, Palloc = 0;
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+
+    ParticleArrays buf[2]{};
+    int cur = 0;
+    bool identity_order = true;  // slot i holds identity i (no sort applied yet)
+    uint32_t* pos = nullptr;     // identity -> slot, valid when pos_valid
+    bool pos_valid = false;
+
+    float* rho = nullptr;
+    float2* spec = nullptr;
+    float* phi = nullptr;
+    float2* force = nullptr;
+    float* kq = nullptr;
+    float2* tw = nullptr;
+    double* diag = nullptr;
+
+    cpm::RadixScratch rs{};
+    int gran = 5, sort_bits = 0, sort_interval = 0;
+    int64_t steps_since_sort = 0;
+    bool sort_due = false;
+
+    float* stage[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaEvent_t stage_ready[2] = {nullptr, nullptr};
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    int stage_slot = 0;
+    std::mutex ticket_mu;
+    std::deque<std::pair<uint64_t, cudaEvent_t>> tickets;
+    std::vector<cudaEvent_t> event_pool;
+    uint64_t next_ticket = 1;
+
+    bool profiling = false;
+    cudaEvent_t ev[kNumStages + 1] = {};
+    bool have_times = false;
+    bool sorted_in_profiled_step = false;
+
+    bool use_graph = true;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+
+    std::string err;
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int now = -1;
+        if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+    }
+};
+
+int finish(cosmos_pm* h, int rc) {
+    if (rc != COSMOS_OK && h) h->err = cpm::last_error_message();
+    return rc;
+}
+
+template <class T>
+int dalloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    if (cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return cpm::fail(COSMOS_ERR_NOMEM, "device allocation of " + std::to_string(n * sizeof(T)) + " bytes failed");
+    }
+    return COSMOS_OK;
+}
+
+ParticleArrays& state(cosmos_pm* h) { return h->buf[h->cur]; }
+
+int sort_now(cosmos_pm* h);
+
+// One step's kernels on stream st, for the buffer parity `cur`.
+int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
+    ParticleArrays& p = state(h);
+    const size_t NN = size_t(h->N) * h->N;
+    auto rec = [&](int i) -> int {
+        if (profile) CPM_CUDA(cudaEventRecord(h->ev[i], st));
+        return COSMOS_OK;
+    };
+    CPM_TRY(rec(kStDeposit));
+    CPM_CUDA(cudaMemsetAsync(h->rho, 0, NN * sizeof(float), st));
+    CPM_CUDA(cpm::launch_deposit_global(p, h->P, h->rho, h->N, h->cic, h->nsm, st));
+    CPM_TRY(rec(kStRows));
+    CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
+    // the three FFT passes are timed together (rows, cols, inverse rows)
+    CPM_TRY(rec(kStForce));
+    CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
+    CPM_TRY(rec(kStIntegrate));
+    CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
+    CPM_TRY(rec(kStSort));
+    return COSMOS_OK;
+}
+
+int get_graph(cosmos_pm* h, cudaGraphExec_t* out) {
+    cudaGraphExec_t& g = h->graph[h->cur];
+    if (!g) {
+        cudaGraph_t graph = nullptr;
+        CPM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_step_body(h, h->stream, false);
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (rc != COSMOS_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return cpm::fail(COSMOS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        const cudaError_t ie = cudaGraphInstantiate(&g, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            g = nullptr;
+            return cpm::fail(COSMOS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        }
+    }
+    *out = g;
+    return COSMOS_OK;
+}
+
+int enqueue_step(cosmos_pm* h) {
+    bool sorted = false;
+    if (h->sort_interval > 0 && (h->sort_due || h->steps_since_sort >= h->sort_interval)) {
+        if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kNumStages], h->stream));
+        CPM_TRY(sort_now(h));
+        sorted = true;
+    }
+    if (h->profiling) {
+        CPM_TRY(enqueue_step_body(h, h->stream, true));
+        h->have_times = true;
+        h->sorted_in_profiled_step = sorted;
+    } else if (h->use_graph) {
+        cudaGraphExec_t g = nullptr;
+        CPM_TRY(get_graph(h, &g));
+        CPM_CUDA(cudaGraphLaunch(g, h->stream));
+    } else {
+        CPM_TRY(enqueue_step_body(h, h->stream, false));
+    }
+    ++h->steps_since_sort;
+    return COSMOS_OK;
+}
+
+// Stable sort of the first Pq slots by tile key; trailing P % 4 particles keep
+// their slots (the step never touches them, like the reference).
+int sort_now(cosmos_pm* h) {
+    cudaStream_t st = h->stream;
+    ParticleArrays& src = h->buf[h->cur];
+    ParticleArrays& dst = h->buf[h->cur ^ 1];
+    CPM_CUDA(cpm::launch_tile_keys(src.x, src.y, h->Pq, h->N, h->gran, h->rs.keys[0], st));
+    CPM_CUDA(cpm::launch_iota(h->rs.vals[0], h->P, st));
+    int which = 0;
+    CPM_CUDA(cpm::launch_radix_sort(h->rs, h->Pq, h->sort_bits, &which, st));
+    if (which != 0 && h->P > h->Pq)  // trailing identities ride along unsorted
+        CPM_CUDA(cudaMemcpyAsync(h->rs.vals[which] + h->Pq, h->rs.vals[0] + h->Pq, (h->P - h->Pq) * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToDevice, st));
+    CPM_CUDA(cpm::launch_permute(src, dst, h->rs.vals[which], h->P, st));
+    h->cur ^= 1;
+    h->identity_order = false;
+    h->pos_valid = false;
+    h->steps_since_sort = 0;
+    h->sort_due = false;
+    return COSMOS_OK;
+}
+
+int ensure_pos(cosmos_pm* h) {
+    if (h->identity_order || h->pos_valid) return COSMOS_OK;
+    CPM_CUDA(cpm::launch_invert(state(h).id, h->pos, h->P, h->stream));
+    h->pos_valid = true;
+    return COSMOS_OK;
+}
+
+int check_range(cosmos_pm* h, int64_t count, int64_t offset) {
+    if (count < 0 || offset < 0 || offset + count > h->P)
+        return cpm::fail(COSMOS_ERR_RANGE, "particle range [" + std::to_string(offset) + ", " +
+                                               std::to_string(offset + count) + ") outside [0, " + std::to_string(h->P) +
+                                               ")");
+    return COSMOS_OK;
+}
+
+int default_sort_interval(int64_t P, int N) {
+    (void)P;
+    (void)N;
+    return 0;  // the global-atomic kernels do not use the tile order
+}
+
+void destroy_all(cosmos_pm* h) {
+    DeviceGuard g(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    for (auto& b : h->buf) {
+        cudaFree(b.x);
+        cudaFree(b.y);
+        cudaFree(b.xo);
+        cudaFree(b.yo);
+        cudaFree(b.m);
+        cudaFree(b.id);
+    }
+    cudaFree(h->pos);
+    cudaFree(h->rho);
+    cudaFree(h->spec);
+    cudaFree(h->phi);
+    cudaFree(h->force);
+    cudaFree(h->kq);
+    cudaFree(h->tw);
+    cudaFree(h->diag);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(h->rs.keys[i]);
+        cudaFree(h->rs.vals[i]);
+        cudaFree(h->stage[i][0]);
+        cudaFree(h->stage[i][1]);
+        if (h->stage_ready[i]) cudaEventDestroy(h->stage_ready[i]);
+        if (h->stage_done[i]) cudaEventDestroy(h->stage_done[i]);
+        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+    }
+    cudaFree(h->rs.counts);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& t : h->tickets) cudaEventDestroy(t.second);
+    for (auto e : h->event_pool) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+}
+
+int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
+    if (!cfg || !out) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const int N = cfg->lattice_n;
+    if (N < 16 || N > 8192 || (N & (N - 1)) != 0)
+        return cpm::fail(COSMOS_ERR_INVALID, "lattice_n must be a power of two in [16, 8192]");
+    if (cfg->deposit != COSMOS_DEPOSIT_NGP && cfg->deposit != COSMOS_DEPOSIT_CIC)
+        return cpm::fail(COSMOS_ERR_INVALID, "deposit must be COSMOS_DEPOSIT_NGP or COSMOS_DEPOSIT_CIC");
+    if (cfg->num_particles < 0 || cfg->num_particles > int64_t(0xFFFFFFF0u))
+        return cpm::fail(COSMOS_ERR_INVALID, "num_particles must be in [0, 2^32 - 16]");
+    if (!std::isfinite(cfg->dt) || !std::isfinite(cfg->gravity_multiplier))
+        return cpm::fail(COSMOS_ERR_INVALID, "dt and gravity_multiplier must be finite");
+    if (cfg->force_mode != COSMOS_FORCE_GRADIENT)
+        return cpm::fail(COSMOS_ERR_INVALID, "force_mode: only COSMOS_FORCE_GRADIENT is available");
+    if (cfg->sort_granularity > 13 || (cfg->sort_granularity >= 0 && (N >> cfg->sort_granularity) < 1))
+        return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity out of range");
+    int ndev = 0;
+    CPM_CUDA(cudaGetDeviceCount(&ndev));
+    if (cfg->device < 0 || cfg->device >= ndev) return cpm::fail(COSMOS_ERR_INVALID, "device ordinal out of range");
+
+    cosmos_pm* h = new cosmos_pm;
+    h->cfg = *cfg;
+    h->N = N;
+    h->logN = cpm::ilog2(N);
+    h->cic = cfg->deposit == COSMOS_DEPOSIT_CIC;
+    h->device = cfg->device;
+    h->P = cfg->num_particles;
+    h->Pq = (h->P / 4) * 4;
+    h->Palloc = ((h->P + 3) / 4) * 4;
+    h->use_graph = cfg->use_graph != 0;
+    h->gran = cfg->sort_granularity >= 0 ? cfg->sort_granularity : (N >= 64 ? 5 : 2);
+    {
+        const int T = N >> h->gran;
+        h->sort_bits = 2 * cpm::ilog2(T) + 1;
+    }
+    h->sort_interval = cfg->sort_interval >= 0 ? cfg->sort_interval : default_sort_interval(h->P, N);
+
+    DeviceGuard guard(h->device);
+    auto bail = [&](int rc) {
+        destroy_all(h);
+        delete h;
+        return rc;
+    };
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "device query"));
+    h->nsm = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(cpm::fail(COSMOS_ERR_CUDA, "stream creation"));
+    for (auto& e : h->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "event creation"));
+    for (int i = 0; i < 2; ++i) {
+        if (cudaEventCreateWithFlags(&h->stage_ready[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->stage_done[i], cudaEventDisableTiming) != cudaSuccess)
+            return bail(cpm::fail(COSMOS_ERR_CUDA, "event creation"));
+    }
+    const size_t NN = size_t(N) * N;
+    const size_t Pa = size_t(h->Palloc);
+    int rc = COSMOS_OK;
+    for (int b = 0; b < 2 && rc == COSMOS_OK; ++b) {
+        ParticleArrays& a = h->buf[b];
+        if ((rc = dalloc(&a.x, Pa)) || (rc = dalloc(&a.y, Pa)) || (rc = dalloc(&a.xo, Pa)) ||
+            (rc = dalloc(&a.yo, Pa)) || (rc = dalloc(&a.m, Pa)) || (rc = dalloc(&a.id, Pa)))
+            break;
+    }
+    if (rc == COSMOS_OK) {
+        h->rs.grid = cpm::radix_grid(h->Pq, h->nsm);
+        if ((rc = dalloc(&h->pos, Pa)) || (rc = dalloc(&h->rho, NN)) || (rc = dalloc(&h->spec, NN / 2)) ||
+            (rc = dalloc(&h->phi, NN)) || (rc = dalloc(&h->force, NN)) ||
+            (rc = dalloc(&h->kq, size_t(N / 2 + 1) * (N / 2 + 1))) || (rc = dalloc(&h->tw, size_t(N))) ||
+            (rc = dalloc(&h->diag, 4)) || (rc = dalloc(&h->rs.keys[0], Pa)) || (rc = dalloc(&h->rs.keys[1], Pa)) ||
+            (rc = dalloc(&h->rs.vals[0], Pa)) || (rc = dalloc(&h->rs.vals[1], Pa)) ||
+            (rc = dalloc(&h->rs.counts, cpm::radix_counts_elems(h->rs.grid))))
+            ;
+    }
+    if (rc != COSMOS_OK) return bail(rc);
+    // zero state; identities; filter
+    for (int b = 0; b < 2; ++b) {
+        ParticleArrays& a = h->buf[b];
+        for (float* f : {a.x, a.y, a.xo, a.yo, a.m})
+            if (cudaMemsetAsync(f, 0, Pa * sizeof(float), h->stream) != cudaSuccess)
+                return bail(cpm::fail(COSMOS_ERR_CUDA, "memset"));
+    }
+    if (cpm::launch_iota(h->buf[0].id, h->Palloc, h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->rho, 0, NN * sizeof(float), h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->phi, 0, NN * sizeof(float), h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->force, 0, NN * sizeof(float2), h->stream) != cudaSuccess)
+        return bail(cpm::fail(COSMOS_ERR_CUDA, "initialisation"));
+    if (cpm::prepare_conv_passes(N) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "kernel attributes"));
+    if ((rc = cpm::build_filter(N, h->cic, h->kq, h->tw, h->stream)) != COSMOS_OK) return bail(rc);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "create sync"));
+    *out = h;
+    return COSMOS_OK;
+}
+
+int set_particles_impl(cosmos_pm* h, const float* x, const float* y, const float* xo, const float* yo, const float* m,
+                       int64_t count, int64_t offset) {
+    CPM_TRY(check_range(h, count, offset));
+    if (count == 0) return COSMOS_OK;
+    if (!x || !y) return cpm::fail(COSMOS_ERR_INVALID, "x and y are required");
+    cudaStream_t st = h->stream;
+    ParticleArrays& p = state(h);
+    const size_t bytes = size_t(count) * sizeof(float);
+    const float* srcs[5] = {x, y, xo ? xo : x, yo ? yo : y, m};
+    float* dsts[5] = {p.x, p.y, p.xo, p.yo, p.m};
+    if (h->identity_order) {
+        for (int i = 0; i < 5; ++i)
+            if (srcs[i]) CPM_CUDA(cudaMemcpyAsync(dsts[i] + offset, srcs[i], bytes, cudaMemcpyHostToDevice, st));
+    } else {
+        CPM_TRY(ensure_pos(h));
+        float* tmp = nullptr;
+        if (cudaMallocAsync(&tmp, bytes, st) != cudaSuccess) {
+            cudaGetLastError();
+            return cpm::fail(COSMOS_ERR_NOMEM, "staging allocation");
+        }
+        for (int i = 0; i < 5; ++i) {
+            if (!srcs[i]) continue;
+            CPM_CUDA(cudaMemcpyAsync(tmp, srcs[i], bytes, cudaMemcpyHostToDevice, st));
+            CPM_CUDA(cpm::launch_scatter_by_id(tmp, h->pos, offset, count, dsts[i], st));
+        }
+        CPM_CUDA(cudaFreeAsync(tmp, st));
+    }
+    CPM_CUDA(cudaStreamSynchronize(st));
+    h->sort_due = true;
+    return COSMOS_OK;
+}
+
+int get_particles_impl(cosmos_pm* h, float* x, float* y, float* xo, float* yo, float* m, int64_t count,
+                       int64_t offset) {
+    CPM_TRY(check_range(h, count, offset));
+    if (count == 0) return COSMOS_OK;
+    cudaStream_t st = h->stream;
+    ParticleArrays& p = state(h);
+    const size_t bytes = size_t(count) * sizeof(float);
+    float* dsts[5] = {x, y, xo, yo, m};
+    const float* srcs[5] = {p.x, p.y, p.xo, p.yo, p.m};
+    if (h->identity_order) {
+        for (int i = 0; i < 5; ++i)
+            if (dsts[i]) CPM_CUDA(cudaMemcpyAsync(dsts[i], srcs[i] + offset, bytes, cudaMemcpyDeviceToHost, st));
+    } else {
+        CPM_TRY(ensure_pos(h));
+        float* tmp = nullptr;
+        if (cudaMallocAsync(&tmp, bytes, st) != cudaSuccess) {
+            cudaGetLastError();
+            return cpm::fail(COSMOS_ERR_NOMEM, "staging allocation");
+        }
+        for (int i = 0; i < 5; ++i) {
+            if (!dsts[i]) continue;
+            CPM_CUDA(cpm::launch_gather_by_id(srcs[i], h->pos, offset, count, tmp, st));
+            CPM_CUDA(cudaMemcpyAsync(dsts[i], tmp, bytes, cudaMemcpyDeviceToHost, st));
+            CPM_CUDA(cudaStreamSynchronize(st));
+        }
+        CPM_CUDA(cudaFreeAsync(tmp, st));
+    }
+    CPM_CUDA(cudaStreamSynchronize(st));
+    return COSMOS_OK;
+}
+
+int positions_async_impl(cosmos_pm* h, float* hx, float* hy, int ordered, uint64_t* ticket) {
+    if (!hx || !hy || !ticket) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    const int s = h->stage_slot;
+    h->stage_slot ^= 1;
+    cudaStream_t st = h->stream;
+    const size_t bytes = size_t(h->P) * sizeof(float);
+    if (!h->stage[s][0]) {
+        CPM_TRY(dalloc(&h->stage[s][0], size_t(h->Palloc)));
+        CPM_TRY(dalloc(&h->stage[s][1], size_t(h->Palloc)));
+    }
+    // the previous readback from this staging slot must have left the device
+    CPM_CUDA(cudaStreamWaitEvent(st, h->stage_done[s], 0));
+    ParticleArrays& p = state(h);
+    if (ordered && !h->identity_order) {
+        CPM_CUDA(cpm::launch_unpermute(p.x, p.id, h->P, h->stage[s][0], st));
+        CPM_CUDA(cpm::launch_unpermute(p.y, p.id, h->P, h->stage[s][1], st));
+    } else {
+        CPM_CUDA(cudaMemcpyAsync(h->stage[s][0], p.x, bytes, cudaMemcpyDeviceToDevice, st));
+        CPM_CUDA(cudaMemcpyAsync(h->stage[s][1], p.y, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    CPM_CUDA(cudaEventRecord(h->stage_ready[s], st));
+    CPM_CUDA(cudaStreamWaitEvent(h->copy_stream, h->stage_ready[s], 0));
+    CPM_CUDA(cudaMemcpyAsync(hx, h->stage[s][0], bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+    CPM_CUDA(cudaMemcpyAsync(hy, h->stage[s][1], bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+    CPM_CUDA(cudaEventRecord(h->stage_done[s], h->copy_stream));
+    cudaEvent_t ev = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(h->ticket_mu);
+        if (!h->event_pool.empty()) {
+            ev = h->event_pool.back();
+            h->event_pool.pop_back();
+        }
+    }
+    if (!ev) CPM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CPM_CUDA(cudaEventRecord(ev, h->copy_stream));
+    std::lock_guard<std::mutex> lk(h->ticket_mu);
+    *ticket = h->next_ticket++;
+    h->tickets.emplace_back(*ticket, ev);
+    return COSMOS_OK;
+}
+
+// Returns the event of a ticket still outstanding, or nullptr if it completed.
+int ticket_query(cosmos_pm* h, uint64_t ticket, bool wait, int32_t* done) {
+    cudaEvent_t ev = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(h->ticket_mu);
+        if (ticket == 0 || ticket >= h->next_ticket) return cpm::fail(COSMOS_ERR_INVALID, "unknown ticket");
+        for (auto& t : h->tickets)
+            if (t.first == ticket) ev = t.second;
+    }
+    if (!ev) {  // retired earlier
+        *done = 1;
+        return COSMOS_OK;
+    }
+    cudaError_t e = wait ? cudaEventSynchronize(ev) : cudaEventQuery(ev);
+    if (e == cudaErrorNotReady) {
+        *done = 0;
+        return COSMOS_OK;
+    }
+    if (e != cudaSuccess) return cpm::fail(COSMOS_ERR_CUDA, std::string("ticket: ") + cudaGetErrorString(e));
+    *done = 1;
+    // retire this and every older ticket (same stream, completed in order)
+    std::lock_guard<std::mutex> lk(h->ticket_mu);
+    while (!h->tickets.empty() && h->tickets.front().first <= ticket) {
+        h->event_pool.push_back(h->tickets.front().second);
+        h->tickets.pop_front();
+    }
+    return COSMOS_OK;
+}
+
+}  // namespace
+
+// ================================= C ABI ============================================
+extern "C" {
+
+void cosmos_pm_default_config(cosmos_pm_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->lattice_n = 2048;
+    c->deposit = COSMOS_DEPOSIT_CIC;
+    c->dt = 1e-3f;
+    c->gravity_multiplier = 1.0f;
+    c->num_particles = 0;
+    c->device = 0;
+    c->force_mode = COSMOS_FORCE_GRADIENT;
+    c->sort_interval = -1;
+    c->sort_granularity = -1;
+    c->use_graph = 1;
+}
+
+int cosmos_pm_create(const cosmos_pm_config* cfg, cosmos_pm** out) { return create_impl(cfg, out); }
+
+int cosmos_pm_destroy(cosmos_pm* h) {
+    if (!h) return COSMOS_OK;
+    destroy_all(h);
+    delete h;
+    return COSMOS_OK;
+}
+
+int cosmos_pm_set_particles(cosmos_pm* h, const float* x, const float* y, const float* xo, const float* yo,
+                            const float* m, int64_t count, int64_t offset) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, set_particles_impl(h, x, y, xo, yo, m, count, offset));
+}
+
+int cosmos_pm_get_particles(cosmos_pm* h, float* x, float* y, float* xo, float* yo, float* m, int64_t count,
+                            int64_t offset) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, get_particles_impl(h, x, y, xo, yo, m, count, offset));
+}
+
+int cosmos_pm_clear(cosmos_pm* h) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        ParticleArrays& p = state(h);
+        for (float* f : {p.x, p.y, p.xo, p.yo}) CPM_CUDA(cpm::launch_fill(f, -10.0f, h->P, h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        h->sort_due = true;
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_step(cosmos_pm* h, int32_t nsteps) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    if (nsteps < 0) return finish(h, cpm::fail(COSMOS_ERR_INVALID, "nsteps < 0"));
+    DeviceGuard g(h->device);
+    for (int i = 0; i < nsteps; ++i) {
+        const int rc = enqueue_step(h);
+        if (rc != COSMOS_OK) return finish(h, rc);
+    }
+    return COSMOS_OK;
+}
+
+int cosmos_pm_synchronize(cosmos_pm* h) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->copy_stream));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_get_positions_async(cosmos_pm* h, float* hx, float* hy, int32_t ordered, uint64_t* ticket) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, positions_async_impl(h, hx, hy, ordered, ticket));
+}
+
+int cosmos_pm_poll(cosmos_pm* h, uint64_t ticket, int32_t* done) {
+    if (!h || !done) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    return ticket_query(h, ticket, false, done);
+}
+
+int cosmos_pm_wait(cosmos_pm* h, uint64_t ticket) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    int32_t done = 0;
+    return finish(h, ticket_query(h, ticket, true, &done));
+}
+
+int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        cudaStream_t st = h->stream;
+        ParticleArrays& p = state(h);
+        switch (stage_id) {
+            case COSMOS_STAGE_DEPOSIT:
+                CPM_CUDA(cudaMemsetAsync(h->rho, 0, size_t(h->N) * h->N * sizeof(float), st));
+                CPM_CUDA(cpm::launch_deposit_global(p, h->P, h->rho, h->N, h->cic, h->nsm, st));
+                break;
+            case COSMOS_STAGE_POTENTIAL:
+                CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
+                break;
+            case COSMOS_STAGE_FORCE:
+                CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
+                break;
+            case COSMOS_STAGE_INTEGRATE:
+                CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
+                break;
+            default:
+                return cpm::fail(COSMOS_ERR_INVALID, "unknown stage");
+        }
+        CPM_CUDA(cudaStreamSynchronize(st));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_get_field(cosmos_pm* h, int32_t field, float* host) {
+    if (!h || !host) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        const size_t NN = size_t(h->N) * h->N;
+        const void* src = nullptr;
+        size_t bytes = NN * sizeof(float);
+        if (field == COSMOS_FIELD_DENSITY) src = h->rho;
+        else if (field == COSMOS_FIELD_POTENTIAL) src = h->phi;
+        else if (field == COSMOS_FIELD_FORCE) { src = h->force; bytes *= 2; }
+        else return cpm::fail(COSMOS_ERR_INVALID, "unknown field");
+        CPM_CUDA(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_set_field(cosmos_pm* h, int32_t field, const float* host) {
+    if (!h || !host) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        const size_t NN = size_t(h->N) * h->N;
+        void* dst = nullptr;
+        size_t bytes = NN * sizeof(float);
+        if (field == COSMOS_FIELD_DENSITY) dst = h->rho;
+        else if (field == COSMOS_FIELD_POTENTIAL) dst = h->phi;
+        else if (field == COSMOS_FIELD_FORCE) { dst = h->force; bytes *= 2; }
+        else return cpm::fail(COSMOS_ERR_INVALID, "unknown field");
+        CPM_CUDA(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_sort(cosmos_pm* h, uint32_t* perm) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        CPM_TRY(sort_now(h));
+        if (perm)
+            CPM_CUDA(cudaMemcpyAsync(perm, state(h).id, size_t(h->P) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                     h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_tile_keys(cosmos_pm* h, const float* x, const float* y, int64_t count, int32_t gran, uint32_t* keys) {
+    if (!h || !x || !y || !keys) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        if (count <= 0) return COSMOS_OK;
+        if (gran < 0 || (h->N >> gran) < 1 || gran > 13) return cpm::fail(COSMOS_ERR_INVALID, "granularity");
+        cudaStream_t st = h->stream;
+        float *dx = nullptr, *dy = nullptr;
+        uint32_t* dk = nullptr;
+        if (cudaMallocAsync(&dx, count * sizeof(float), st) != cudaSuccess ||
+            cudaMallocAsync(&dy, count * sizeof(float), st) != cudaSuccess ||
+            cudaMallocAsync(&dk, count * sizeof(uint32_t), st) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFreeAsync(dx, st);
+            cudaFreeAsync(dy, st);
+            cudaFreeAsync(dk, st);
+            return cpm::fail(COSMOS_ERR_NOMEM, "staging allocation");
+        }
+        CPM_CUDA(cudaMemcpyAsync(dx, x, count * sizeof(float), cudaMemcpyHostToDevice, st));
+        CPM_CUDA(cudaMemcpyAsync(dy, y, count * sizeof(float), cudaMemcpyHostToDevice, st));
+        CPM_CUDA(cpm::launch_tile_keys(dx, dy, count, h->N, gran, dk, st));
+        CPM_CUDA(cudaMemcpyAsync(keys, dk, count * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CPM_CUDA(cudaFreeAsync(dx, st));
+        CPM_CUDA(cudaFreeAsync(dy, st));
+        CPM_CUDA(cudaFreeAsync(dk, st));
+        CPM_CUDA(cudaStreamSynchronize(st));
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_diagnostics(cosmos_pm* h, double* ke, double* pe, double* px, double* py) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        double out[4];
+        CPM_CUDA(cpm::launch_diagnostics(state(h), h->P, h->phi, h->N, h->cfg.dt, h->diag, h->stream));
+        CPM_CUDA(cudaMemcpyAsync(out, h->diag, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+        CPM_CUDA(cudaStreamSynchronize(h->stream));
+        if (ke) *ke = out[0];
+        if (pe) *pe = out[1];
+        if (px) *px = out[2];
+        if (py) *py = out[3];
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_set_profiling(cosmos_pm* h, int32_t enabled) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    h->profiling = enabled != 0;
+    h->have_times = false;
+    return COSMOS_OK;
+}
+
+int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n) {
+    if (!h || !times || !n) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    DeviceGuard g(h->device);
+    auto impl = [&]() -> int {
+        if (!h->have_times) return cpm::fail(COSMOS_ERR_STATE, "no profiled step yet");
+        CPM_CUDA(cudaEventSynchronize(h->ev[kStSort]));
+        // entries: deposit, fft (all three passes), -, -, force, integrate, sort
+        float t[kNumStages] = {0};
+        CPM_CUDA(cudaEventElapsedTime(&t[0], h->ev[kStDeposit], h->ev[kStRows]));
+        CPM_CUDA(cudaEventElapsedTime(&t[1], h->ev[kStRows], h->ev[kStForce]));
+        CPM_CUDA(cudaEventElapsedTime(&t[4], h->ev[kStForce], h->ev[kStIntegrate]));
+        CPM_CUDA(cudaEventElapsedTime(&t[5], h->ev[kStIntegrate], h->ev[kStSort]));
+        if (h->sorted_in_profiled_step) CPM_CUDA(cudaEventElapsedTime(&t[6], h->ev[kNumStages], h->ev[kStDeposit]));
+        const int cnt = *n < kNumStages ? *n : kNumStages;
+        for (int i = 0; i < cnt; ++i) times[i] = t[i];
+        *n = cnt;
+        return COSMOS_OK;
+    };
+    return finish(h, impl());
+}
+
+int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream) {
+    if (!h || !stream) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    *stream = reinterpret_cast<uint64_t>(h->stream);
+    return COSMOS_OK;
+}
+
+int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
+    if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    // deposit + FFT passes + gradient + integrate (the density clear is a memset node)
+    *launches = 1 + cpm::conv_launches_per_step() + 1 + 1;
+    return COSMOS_OK;
+}
+
+const char* cosmos_pm_last_error(cosmos_pm* h) {
+    if (h) return h->err.c_str();
+    return cpm::last_error_message();
+}
+
+const char* cosmos_pm_version(void) { return "0.1.0"; }
+
+}  // extern "C"

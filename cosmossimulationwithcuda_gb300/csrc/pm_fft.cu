@@ -1,0 +1,359 @@
+// FFT convolution passes of the particle-mesh step and the FP64 filter build.
+//
+// The reference convolves the density with the Green's lattice through
+// cuFFT: copy to complex (CosmosCuda.cuh:596-612), forward C2C FFT (:1266),
+// multiply by FFT(G) (:149-173), divide by the FFT of the mass-assignment
+// kernel with 0.001 regularisation (:120-148), inverse C2C FFT (:1291), shift
+// by N/2 and divide by N^2 (:333-355).  With G real and even and the
+// assignment kernel a (shifted) delta or 2x2 box, all of that collapses to
+//     phi = IFFT2( FFT2(rho) * K ),   K = Ghat * W / (W^2 + 0.001) / N^2,
+// W = 1 (NGP) or cos(pi kx/N) cos(pi ky/N) (CIC), K real and even in both
+// axes.  The N/2 shifts of the reference cancel (the (-1)^(kx+ky) factor of
+// the assignment kernel's spectrum undoes k_shiftLattice).
+//
+// Passes (all hand-written, no cuFFT):
+//  1. k_rows_r2c   : B density rows per CTA -> real FFT of each row (one
+//                    N/2-point complex FFT + split), stored TRANSPOSED as
+//                    spec[kx][y] so that the column pass reads contiguous
+//                    lines.  kx = 0 and kx = N/2 (both real along x) share
+//                    line 0 as X0 + i*XN/2.
+//  2. k_cols_conv  : per line kx: forward FFT over y, multiply by K (line 0
+//                    unpacks / repacks its two real spectra), inverse FFT over
+//                    y, written back in place.
+//  3. k_rows_c2r   : B rows per CTA, Hermitian pre-split + N/2-point inverse
+//                    FFT, the potential row written as float2 pairs.
+// The filter build runs passes 1-2 in FP64 on the Green's lattice.
+#include <cmath>
+#include <vector>
+
+#include "fft_engine.cuh"
+#include "pm_internal.h"
+
+namespace cpm {
+
+// ---- launch shapes ------------------------------------------------------------------
+template <class T, int N>
+struct RowShape {
+    static constexpr int M = N / 2;
+    static constexpr int Bf = (N <= 256) ? 16 : (N <= 2048 ? 8 : 4);
+    static constexpr int B = (sizeof(T) == 8) ? (Bf / 2) : Bf;  // rows per CTA
+    static constexpr int NT = (N <= 64) ? 64 : (N <= 256 ? 128 : (N <= 4096 ? 256 : 512));
+    static constexpr size_t smem = size_t(B) * LinePad<M>::value * sizeof(cplx_t<T>);
+};
+
+template <class T, int N>
+struct ColShape {
+    static constexpr int M = N / 2;
+    static constexpr int B = (N <= 256) ? 8 : (N <= 512 ? 4 : (N <= 2048 ? 2 : 1));  // lines per CTA
+    static constexpr int NT = (N <= 128) ? 64 : (N <= 2048 ? 256 : 512);
+    static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);
+};
+
+// ---- pass 1: rows, real -> half spectrum, transposed store --------------------------------
+template <class T, int N, int B, int NT>
+__global__ void __launch_bounds__(NT) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
+                                                 const cplx_t<T>* __restrict__ tw) {
+    using C = cplx_t<T>;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<M>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int y0 = int(blockIdx.x) * B;
+    // Row b as M complex values z[n] = (x[2n], x[2n+1]).
+    const C* rows = reinterpret_cast<const C*>(in + size_t(y0) * N);
+    auto src = [rows](int line, int i) { return rows[line * M + i]; };
+    auto dst = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
+    fft_lines<M, B, NT, -1, C>(s, src, dst, tw, 2);
+    // X[k] = (Z[k] + conj Z[M-k])/2 - i/2 W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i/N)
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int k = idx / B;
+        const int b = idx - k * B;
+        const C zk = s[b * LP + pad16(k)];
+        C out;
+        if (k == 0) {
+            out = cmake<C>(zk.x + zk.y, zk.x - zk.y);  // (X[0], X[N/2]) packed
+        } else {
+            const C zm = cconj(s[b * LP + pad16(M - k)]);
+            const C a = cadd(zk, zm);
+            const C wd = cmul(tw[k], csub(zk, zm));
+            out = cmake<C>(T(0.5) * (a.x + wd.y), T(0.5) * (a.y - wd.x));
+        }
+        spec[size_t(k) * N + y0 + b] = out;
+    }
+}
+
+// ---- pass 2: columns, forward FFT x K x inverse FFT ----------------------------------------
+// kq: (N/2+1) x (N/2+1) floats, kq[kx*(M+1) + min(ky, N-ky)].
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
+                                                  const float2* __restrict__ tw) {
+    using C = float2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<N>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int kx0 = int(blockIdx.x) * B;
+    C* lines = spec + size_t(kx0) * N;
+    auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
+    auto gstore = [lines](int line, int i, C v) { lines[size_t(line) * N + i] = v; };
+    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
+    auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
+    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    for (int idx = threadIdx.x; idx < B * (M + 1); idx += NT) {
+        const int b = idx / (M + 1);
+        const int ky = idx - b * (M + 1);
+        const int kx = kx0 + b;
+        const int i1 = b * LP + pad16(ky);
+        const int i2 = b * LP + pad16((N - ky) & (N - 1));
+        if (kx != 0) {
+            const float kv = __ldg(kq + size_t(kx) * (M + 1) + ky);
+            s[i1] = cscale(s[i1], kv);
+            if (ky != 0 && ky != M) s[i2] = cscale(s[i2], kv);
+        } else {
+            // line 0 holds P = X0 + i XM with X0, XM Hermitian in ky:
+            // P' = (K0+KM)/2 * P[ky] + (K0-KM)/2 * conj(P[N-ky])
+            const float k0 = __ldg(kq + ky);
+            const float km = __ldg(kq + size_t(M) * (M + 1) + ky);
+            const float p = 0.5f * (k0 + km), q = 0.5f * (k0 - km);
+            const C z1 = s[i1], z2 = s[i2];
+            s[i1] = cadd(cscale(z1, p), cscale(cconj(z2), q));
+            if (ky != 0 && ky != M) s[i2] = cadd(cscale(z2, p), cscale(cconj(z1), q));
+        }
+    }
+    __syncthreads();
+    fft_lines<N, B, NT, +1, C>(s, sload, gstore, tw, 1);
+}
+
+// FP64 forward column FFT for the filter build: writes the real part of the
+// 2-D spectrum of a real, even input as ghat[kx][ky], kx in [0, N/2], ky in [0, N).
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT) k_cols_fwd_real64(const double2* __restrict__ spec, double* __restrict__ ghat,
+                                                        const double2* __restrict__ tw) {
+    using C = double2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<N>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int kx0 = int(blockIdx.x) * B;
+    const C* lines = spec + size_t(kx0) * N;
+    auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
+    auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
+    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    for (int idx = threadIdx.x; idx < B * N; idx += NT) {
+        const int b = idx / N;
+        const int ky = idx - b * N;
+        const int kx = kx0 + b;
+        const C z1 = s[b * LP + pad16(ky)];
+        if (kx != 0) {
+            ghat[size_t(kx) * N + ky] = z1.x;
+        } else {
+            const C z2 = s[b * LP + pad16((N - ky) & (N - 1))];
+            ghat[ky] = 0.5 * (z1.x + z2.x);                     // spectrum of line kx = 0
+            ghat[size_t(M) * N + ky] = 0.5 * (z1.y + z2.y);     // spectrum of line kx = N/2
+        }
+    }
+}
+
+// ---- pass 3: rows, half spectrum (transposed) -> real potential rows -----------------------
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
+                                                 const float2* __restrict__ tw) {
+    using C = float2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<M>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int y0 = int(blockIdx.x) * B;
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int k = idx / B;
+        const int b = idx - k * B;
+        s[b * LP + pad16(k)] = spec[size_t(k) * N + y0 + b];
+    }
+    __syncthreads();
+    // Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k])  (twice the
+    // spectrum of z[n] = x[2n] + i x[2n+1]); pairs (k, M-k) in one thread.
+    constexpr int H = M / 2 + 1;
+    for (int idx = threadIdx.x; idx < H * B; idx += NT) {
+        const int b = idx / H;
+        const int k = idx - b * H;
+        C* row = s + b * LP;
+        if (k == 0) {
+            const C x = row[0];  // (X[0], X[N/2])
+            row[0] = cmake<C>(x.x + x.y, x.x - x.y);
+        } else {
+            const C xk = row[pad16(k)];
+            const C xm = row[pad16(M - k)];
+            {
+                const C a = cadd(xk, cconj(xm));
+                const C d = cmul(cconj(tw[k]), csub(xk, cconj(xm)));
+                row[pad16(k)] = cmake<C>(a.x - d.y, a.y + d.x);
+            }
+            if (k != M - k) {
+                const C a = cadd(xm, cconj(xk));
+                const C d = cmul(cconj(tw[M - k]), csub(xm, cconj(xk)));
+                row[pad16(M - k)] = cmake<C>(a.x - d.y, a.y + d.x);
+            }
+        }
+    }
+    __syncthreads();
+    float2* orow = reinterpret_cast<float2*>(out + size_t(y0) * N);
+    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
+    auto gstore = [orow](int line, int i, C v) { orow[size_t(line) * M + i] = v; };
+    fft_lines<M, B, NT, +1, C>(s, sload, gstore, tw, 2);
+}
+
+// ---- filter build helpers ----------------------------------------------------------------
+// Green's lattice G(i, j) = 1/r with minimum-image distances and 3.0 at
+// r <= 0.5 (CosmosCuda.cuh:100-117), in FP64.
+__global__ void k_green64(double* __restrict__ g, int N) {
+    const int64_t NN = int64_t(N) * N;
+    for (int64_t idx = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; idx < NN; idx += int64_t(gridDim.x) * blockDim.x) {
+        const int i = int(idx % N), j = int(idx / N);
+        const double dx = double(i <= N / 2 ? i : i - N);
+        const double dy = double(j <= N / 2 ? j : j - N);
+        const double r = sqrt(dx * dx + dy * dy);
+        g[idx] = r > 0.5 ? 1.0 / r : 3.0;
+    }
+}
+
+// K = Ghat * W / (W^2 + 0.001) / N^2 on the quarter (kx, ky) in [0, N/2]^2.
+__global__ void k_build_kq(const double* __restrict__ ghat, float* __restrict__ kq, int N, int cic) {
+    const int M = N / 2;
+    const int total = (M + 1) * (M + 1);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / (M + 1), ky = idx - kx * (M + 1);
+        const double g = ghat[size_t(kx) * N + ky];
+        const double w = cic ? cospi(double(kx) / N) * cospi(double(ky) / N) : 1.0;
+        kq[idx] = float(g * w / (w * w + 0.001) / (double(N) * double(N)));
+    }
+}
+
+// ---- host launchers ------------------------------------------------------------------------
+template <class K>
+static cudaError_t allow_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+}
+
+template <int N>
+static cudaError_t conv_passes_n(const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
+                                 cudaStream_t st) {
+    using RS = RowShape<float, N>;
+    using CS = ColShape<float, N>;
+    k_rows_r2c<float, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_cols_conv<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, CS::smem, st>>>(spec, kq, tw);
+    k_rows_c2r<N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(spec, phi, tw);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t filter_passes_n(const double* g, double2* spec64, double* ghat, const double2* tw64,
+                                   cudaStream_t st) {
+    using RS = RowShape<double, N>;
+    using CS = ColShape<double, N>;
+    cudaError_t e;
+    if ((e = allow_smem(k_rows_r2c<double, N, RS::B, RS::NT>, RS::smem)) != cudaSuccess) return e;
+    if ((e = allow_smem(k_cols_fwd_real64<N, CS::B, CS::NT>, CS::smem)) != cudaSuccess) return e;
+    k_rows_r2c<double, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(g, spec64, tw64);
+    k_cols_fwd_real64<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, CS::smem, st>>>(spec64, ghat, tw64);
+    return cudaGetLastError();
+}
+
+#define CPM_FOR_EACH_N(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+
+template <int N>
+static cudaError_t prepare_conv_n() {
+    using RS = RowShape<float, N>;
+    using CS = ColShape<float, N>;
+    cudaError_t e;
+    if ((e = allow_smem(k_rows_r2c<float, N, RS::B, RS::NT>, RS::smem)) != cudaSuccess) return e;
+    if ((e = allow_smem(k_cols_conv<N, CS::B, CS::NT>, CS::smem)) != cudaSuccess) return e;
+    return allow_smem(k_rows_c2r<N, RS::B, RS::NT>, RS::smem);
+}
+
+// Raises the dynamic shared-memory limit of the FFT kernels of lattice size N
+// on the current device (called once per handle, outside stream capture).
+cudaError_t prepare_conv_passes(int N) {
+    switch (N) {
+#define CPM_CASE(n) \
+    case n:         \
+        return prepare_conv_n<n>();
+        CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
+                               cudaStream_t st) {
+    switch (N) {
+#define CPM_CASE(n) \
+    case n:         \
+        return conv_passes_n<n>(rho, spec, kq, phi, tw, st);
+        CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+int conv_launches_per_step() { return 3; }
+
+// Builds the twiddle tables (host, FP64 std::cos/std::sin) and the filter K.
+int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st) {
+    std::vector<float2> twf(N);
+    std::vector<double2> twd(N);
+    for (int m = 0; m < N; ++m) {
+        const double a = -2.0 * M_PI * double(m) / double(N);
+        twd[m] = make_double2(std::cos(a), std::sin(a));
+        twf[m] = make_float2(float(twd[m].x), float(twd[m].y));
+    }
+    CPM_CUDA(cudaMemcpyAsync(tw_dev, twf.data(), sizeof(float2) * N, cudaMemcpyHostToDevice, st));
+    const size_t NN = size_t(N) * N;
+    const int M = N / 2;
+    double* g = nullptr;
+    double2* spec64 = nullptr;
+    double* ghat = nullptr;
+    double2* tw64 = nullptr;
+    int status = COSMOS_OK;
+    auto cleanup = [&]() {
+        cudaFreeAsync(g, st);
+        cudaFreeAsync(spec64, st);
+        cudaFreeAsync(ghat, st);
+        cudaFreeAsync(tw64, st);
+    };
+    if (cudaMallocAsync(&g, sizeof(double) * NN, st) != cudaSuccess ||
+        cudaMallocAsync(&spec64, sizeof(double2) * size_t(M) * N, st) != cudaSuccess ||
+        cudaMallocAsync(&ghat, sizeof(double) * size_t(M + 1) * N, st) != cudaSuccess ||
+        cudaMallocAsync(&tw64, sizeof(double2) * N, st) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return fail(COSMOS_ERR_NOMEM, "filter build: device allocation failed");
+    }
+    cudaError_t e = cudaMemcpyAsync(tw64, twd.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        k_green64<<<1024, 256, 0, st>>>(g, N);
+        switch (N) {
+#define CPM_CASE(n)                                            \
+    case n:                                                    \
+        e = filter_passes_n<n>(g, spec64, ghat, tw64, st);     \
+        break;
+            CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+            default:
+                e = cudaErrorInvalidValue;
+        }
+    }
+    if (e == cudaSuccess) {
+        k_build_kq<<<1024, 256, 0, st>>>(ghat, kq_dev, N, cic);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) status = fail(COSMOS_ERR_CUDA, std::string("filter build: ") + cudaGetErrorString(e));
+    cleanup();
+    cudaStreamSynchronize(st);
+    return status;
+}
+
+}  // namespace cpm

@@ -1,0 +1,197 @@
+/*
+ * cosmos_pm.h -- C ABI of the GB300 particle-mesh gravity step.
+ *
+ * Drop-in for the hot path of tugrul512bit/CosmosSimulationWithCuda
+ * (CosmosCuda.cuh): the simulation class Universe<K> owns a particle state
+ * (x, y, xOld, yOld, m), builds the 1/r Green's filter once, and advances the
+ * state with the particle-mesh step
+ *     deposit (NGP / CIC) -> 2-D FFT convolution -> gradient -> gather + update.
+ * Every entry point below replaces one part of that class; the comment on each
+ * names the reference code it stands for.
+ *
+ * Conventions
+ *  - Plain C types only: host pointers, sizes in elements, int status codes.
+ *  - Every function returns COSMOS_OK (0) or a negative COSMOS_ERR_* code and
+ *    never exits the process (the reference calls exit() on any CUDA error,
+ *    CosmosCuda.cuh:19-27).  cosmos_pm_last_error() gives a message.
+ *  - The library owns all device memory of a handle; the caller owns every
+ *    host buffer it passes.
+ *  - One host thread per handle at a time, except cosmos_pm_poll(), which may
+ *    be called from any thread.
+ *  - Particle identity: particle i is the i-th element of the arrays given to
+ *    cosmos_pm_set_particles().  The library may keep particles in a different
+ *    order internally (sorted by lattice tile); every get/set call below
+ *    addresses particles by identity unless it says otherwise.
+ *  - Like the reference, only the first 4*floor(P/4) particles take part in
+ *    the step (it walks float4 groups, CosmosCuda.cuh:239-242, 454-471).
+ */
+#ifndef COSMOS_PM_H
+#define COSMOS_PM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define COSMOS_OK 0
+#define COSMOS_ERR_INVALID -1   /* bad argument or configuration */
+#define COSMOS_ERR_CUDA -2      /* a CUDA runtime call failed */
+#define COSMOS_ERR_NOMEM -3     /* device or pinned allocation failed */
+#define COSMOS_ERR_RANGE -4     /* offset/count outside the particle range */
+#define COSMOS_ERR_TIMEOUT -5   /* a bounded device-side wait gave up */
+#define COSMOS_ERR_STATE -6     /* call not valid in the handle's current state */
+
+/* ---- configuration -------------------------------------------------------- */
+/* Mass assignment: NGP = the reference's lowAccuracy=true, CIC = false
+ * (CosmosCuda.cuh:890, deposit :507-515, gather :262-284). */
+#define COSMOS_DEPOSIT_NGP 0
+#define COSMOS_DEPOSIT_CIC 1
+
+/* Force evaluation.
+ *  GRADIENT: potential on the lattice, then the reference's edge-clamped
+ *            4th-order difference (CosmosCuda.cuh:174-229).
+ *  SPECTRAL: the same difference stencil applied in Fourier space with the
+ *            reference's edge clamping restored at the border cells; the
+ *            force comes out of the inverse FFT directly instead of being
+ *            differenced from an FP32 potential (about 100x smaller error
+ *            against FP64 at the same memory traffic). */
+#define COSMOS_FORCE_GRADIENT 0
+#define COSMOS_FORCE_SPECTRAL 1
+
+typedef struct cosmos_pm_config {
+    int32_t lattice_n;          /* N: power of two, 16..8192   (Constants::N, CosmosCuda.cuh:38) */
+    int32_t deposit;            /* COSMOS_DEPOSIT_NGP / _CIC   (Universe ctor lowAccuracy, :881,890) */
+    float dt;                   /* time step                   (Constants::dt, :43) */
+    float gravity_multiplier;   /* force multiplier            (Constants::gravityMultiplier, :45) */
+    int64_t num_particles;      /* P                           (Universe ctor `particles`, :881) */
+    int32_t device;             /* CUDA device ordinal         (cudaDevices[0], :881,970) */
+    int32_t force_mode;         /* COSMOS_FORCE_*  (0 = reference-faithful gradient) */
+    int32_t sort_interval;      /* steps between particle re-sorts; 0 = never sort,
+                                   -1 = library default for this lattice/particle count */
+    int32_t sort_granularity;   /* log2 of the tile edge (cells) used as sort key; -1 = default */
+    int32_t use_graph;          /* 1 = replay each step from a captured CUDA graph */
+    int32_t reserved[7];
+} cosmos_pm_config;
+
+typedef struct cosmos_pm cosmos_pm; /* opaque handle (one Universe) */
+
+/* Fill *cfg with defaults: N=2048, CIC, dt=1e-3, gravity 1, P=0, device 0,
+ * gradient force, library-default sorting, graphs on. */
+void cosmos_pm_default_config(cosmos_pm_config* cfg);
+
+/* Create a simulation: allocates the particle state (zeroed), the lattices and
+ * the filter, and builds the filter in FP64 on the device.  Replaces the
+ * Universe constructor's allocation and filter build (CosmosCuda.cuh:969-1034);
+ * the constructor's random particle fill is not part of it (use
+ * cosmos_pm_set_particles with seeded data). */
+int cosmos_pm_create(const cosmos_pm_config* cfg, cosmos_pm** out);
+
+/* Release everything.  Replaces ~Universe (CosmosCuda.cuh:1396-1427). */
+int cosmos_pm_destroy(cosmos_pm* h);
+
+/* Copy `count` particles from host arrays into identities [offset, offset+count).
+ * Any of x_old, y_old may be NULL (then they are set equal to x, y: zero
+ * velocity); m may be NULL (masses unchanged).  Synchronous.  Replaces the
+ * host-to-device uploads of the constructor and of addGalaxy
+ * (CosmosCuda.cuh:1012-1016, 1151-1155). */
+int cosmos_pm_set_particles(cosmos_pm* h, const float* x, const float* y, const float* x_old,
+                            const float* y_old, const float* m, int64_t count, int64_t offset);
+
+/* Copy particles [offset, offset+count) (by identity) to host arrays; any
+ * pointer may be NULL to skip that array.  Synchronous. */
+int cosmos_pm_get_particles(cosmos_pm* h, float* x, float* y, float* x_old, float* y_old, float* m,
+                            int64_t count, int64_t offset);
+
+/* Park every particle at (-10, -10) with xOld = x, so none is deposited or
+ * moved.  Replaces Universe::clear (CosmosCuda.cuh:1038-1069). */
+int cosmos_pm_clear(cosmos_pm* h);
+
+/* Enqueue `nsteps` particle-mesh steps on the handle's stream and return
+ * without waiting.  One step = scatterMassOnLattice, calcLatticeFft2D,
+ * multiplyLatticeFilterElementwise, calcLatticeIfft2D, multiSampleForces
+ * (CosmosCuda.cuh:1209-1300, loop :1336-1342). */
+int cosmos_pm_step(cosmos_pm* h, int32_t nsteps);
+
+/* Wait until every enqueued step and copy of the handle has finished. */
+int cosmos_pm_synchronize(cosmos_pm* h);
+
+/* Asynchronous readback of the positions after the last enqueued step into
+ * host_x, host_y (P floats each; page-locked memory gives a truly
+ * asynchronous copy).  ordered=1 delivers particle identities in order;
+ * ordered=0 delivers the library's internal order (cheaper; enough for a
+ * renderer).  The step stream does not wait for the copy.  Returns a ticket
+ * for cosmos_pm_poll / cosmos_pm_wait.  New API: the reference has no
+ * position readback (it renders a density frame, CosmosCuda.cuh:1343-1351). */
+int cosmos_pm_get_positions_async(cosmos_pm* h, float* host_x, float* host_y, int32_t ordered,
+                                  uint64_t* ticket);
+
+/* *done = 1 when the copy behind `ticket` has landed in host memory. */
+int cosmos_pm_poll(cosmos_pm* h, uint64_t ticket, int32_t* done);
+
+/* Block until the copy behind `ticket` has landed. */
+int cosmos_pm_wait(cosmos_pm* h, uint64_t ticket);
+
+/* ---- stage-level access (test hooks; the reference's private step methods) */
+#define COSMOS_FIELD_DENSITY 0   /* N*N float: accumulator_d after deposit (:1242) */
+#define COSMOS_FIELD_POTENTIAL 1 /* N*N float: latticeShifted_d (:1297) */
+#define COSMOS_FIELD_FORCE 2     /* N*N*2 float (fx, fy): latticeShiftedForceXY_d (:1298) */
+
+/* Run one stage of the step on the current state.
+ *  COSMOS_STAGE_DEPOSIT   : density from the particles   (scatterMassOnLattice, :1209-1264)
+ *  COSMOS_STAGE_POTENTIAL : potential from the density   (:1265-1297, FFT conv + shift)
+ *  COSMOS_STAGE_FORCE     : force field from the density or potential (:1298)
+ *  COSMOS_STAGE_INTEGRATE : gather + update from the force field (:1299) */
+#define COSMOS_STAGE_DEPOSIT 0
+#define COSMOS_STAGE_POTENTIAL 1
+#define COSMOS_STAGE_FORCE 2
+#define COSMOS_STAGE_INTEGRATE 3
+int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage);
+
+/* Copy a lattice field to / from the host (synchronous). */
+int cosmos_pm_get_field(cosmos_pm* h, int32_t field, float* host);
+int cosmos_pm_set_field(cosmos_pm* h, int32_t field, const float* host);
+
+/* Sort the particles by lattice tile now (stable by identity order within a
+ * tile) and write the resulting internal order: perm[i] = identity of the
+ * particle in internal slot i.  perm may be NULL. */
+int cosmos_pm_sort(cosmos_pm* h, uint32_t* perm);
+
+/* Tile keys the sort uses, computed on the device from host positions: for
+ * testing the key function bit-exactly.  keys: count uint32. */
+int cosmos_pm_tile_keys(cosmos_pm* h, const float* x, const float* y, int64_t count, int32_t granularity,
+                        uint32_t* keys);
+
+/* FP64 diagnostics: kinetic energy sum(m v^2)/2 with v = (x - xOld)/dt, the
+ * momentum sum(m v), over active particles, and the potential energy
+ * sum(m phi(x))/2 sampled from the potential field of the last step (NGP
+ * sample).  No counterpart in the reference. */
+int cosmos_pm_diagnostics(cosmos_pm* h, double* kinetic, double* potential, double* momentum_x,
+                          double* momentum_y);
+
+/* Per-stage device time of the last step run with profiling on (ms), for
+ * benchmarks.  times[i] in the order deposit, fft-rows, fft-columns,
+ * fft-inverse-rows, force, integrate, sort; n = capacity.  Returns the number
+ * of entries written in *n. */
+int cosmos_pm_set_profiling(cosmos_pm* h, int32_t enabled);
+int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n);
+
+/* The cudaStream_t the handle enqueues on (as an integer), for callers that
+ * record their own events around cosmos_pm_step. */
+int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream);
+
+/* Number of kernel launches one step enqueues (for launch accounting). */
+int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
+
+/* Message of the last error on this handle (or the last create failure when
+ * h is NULL).  The string stays valid until the next call on the handle. */
+const char* cosmos_pm_last_error(cosmos_pm* h);
+
+/* Library version, e.g. "0.1.0". */
+const char* cosmos_pm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* COSMOS_PM_H */
