@@ -104,7 +104,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -114,6 +114,13 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def wait_first(self, timeout: float = 5.0):
+        """Block until the sampler has produced its first line (it starts slowly)."""
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.02)
+        self.skip = len(self.lines)
 
     def __exit__(self, *a):
         if self.proc:
@@ -128,7 +135,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "skip", 0):]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -185,7 +192,7 @@ def dist_env():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--particles", type=int, default=None, help="override the particle count (testing)")
@@ -232,17 +239,21 @@ def main():
     sim.set_state(state)
 
     # ---- device-timed throughput (state resident) ----
+    clk = ClockSampler(local).__enter__()
     sim.step(args.warmup)
     sim.synchronize()
+    clk.wait_first()
     e0, e1 = rt.event(), rt.event()
     if ws > 1:
         import torch.distributed as dist
         dist.barrier()
-    with ClockSampler(local) as clk:
+    try:
         rt.record(e0, stream)
         sim.step(args.steps)
         rt.record(e1, stream)
         ms = rt.elapsed_ms(e0, e1)
+    finally:
+        clk.__exit__()
     sim.synchronize()
     if ws > 1:
         import torch
@@ -255,19 +266,29 @@ def main():
 
     # ---- per-stage times (profiled direct launches, events between kernels) ----
     sim.set_profiling(True)
-    prof_steps = 20
-    acc = np.zeros(7)
+    prof_steps = 32
+    names = ["prologue", "fft_conv", "force", "fused_step", "sort"]
+    acc = np.zeros(len(names))
+    sorts = 0
     for _ in range(prof_steps):
         sim.step(1)
-        acc += np.pad(sim.stage_times(), (0, 7))[:7]
+        t = np.pad(sim.stage_times(), (0, len(names)))[:len(names)]
+        acc += t
+        sorts += int(t[4] > 0)
     sim.set_profiling(False)
     sim.synchronize()
-    stage_ms = acc / prof_steps
-    names = ["deposit", "fft_conv", "-", "-", "force", "integrate", "sort"]
-    stages = {n: round(float(t), 5) for n, t in zip(names, stage_ms) if n != "-"}
-    # dominant kernel and its algorithmic bytes per launch
-    algo = {"deposit": 12.0 * P + 4.0 * N * N, "integrate": 32.0 * P + 8.0 * N * N,
-            "fft_conv": 25.0 * N * N, "force": 12.0 * N * N}
+    stage_ms = acc / prof_steps  # sort: amortised per step
+    stages = {n: round(float(t), 5) for n, t in zip(names, stage_ms)}
+    stages["sort_per_sort"] = round(float(acc[4] / max(sorts, 1)), 5)
+    # algorithmic bytes per launch (per step for the FFT passes)
+    algo = {
+        # read x, y, xOld, yOld, m (20 B), write x, y, xOld, yOld (16 B); density clear 4 B/cell,
+        # force window 8 B/cell, density flush 4 B/cell
+        "fused_step": 36.0 * P + 16.0 * N * N,
+        # r2c rows 4+4, columns 4+2+4 (real K on a quarter: 1 B/cell), c2r rows 4+4
+        "fft_conv": 25.0 * N * N,
+        "force": 12.0 * N * N,
+    }
     dom = max(algo, key=lambda k: stages.get(k, 0.0))
     peak, peak_kind = measured_peak_gbs()
     achieved = algo[dom] / (stages[dom] / 1e3) / 1e9

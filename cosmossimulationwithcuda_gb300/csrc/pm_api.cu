@@ -31,7 +31,10 @@ const char* last_error_message() { return g_last_error.c_str(); }
 
 using cpm::ParticleArrays;
 
-enum StageIdx { kStDeposit = 0, kStRows, kStCols, kStRowsInv, kStForce, kStIntegrate, kStSort, kNumStages };
+// Profiling event slots: [prologue deposit] [sort] fft | force | fused step | end
+enum EvIdx { kEvPrologue = 0, kEvSort, kEvFft, kEvForce, kEvFused, kEvEnd, kNumEv };
+// Entries of cosmos_pm_stage_times.
+enum StageIdx { kTPrologue = 0, kTFft, kTForce, kTFused, kTSort, kNumTimes };
 
 struct cosmos_pm {
     cosmos_pm_config cfg{};
@@ -58,6 +61,16 @@ struct cosmos_pm {
     int64_t steps_since_sort = 0;
     bool sort_due = false;
 
+    // tile work items (valid after a sort, until the state is rewritten)
+    uint32_t* tstart = nullptr;
+    uint32_t* tend = nullptr;
+    cpm::WorkItem* items = nullptr;
+    uint32_t* n_items = nullptr;
+    size_t max_items = 0;
+    bool items_valid = false;
+    int tiles_grid = 0;
+    bool density_valid = false;  // rho holds the density of the current positions
+
     float* stage[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     cudaEvent_t stage_ready[2] = {nullptr, nullptr};
     cudaEvent_t stage_done[2] = {nullptr, nullptr};
@@ -68,12 +81,12 @@ struct cosmos_pm {
     uint64_t next_ticket = 1;
 
     bool profiling = false;
-    cudaEvent_t ev[kNumStages + 1] = {};
+    cudaEvent_t ev[kNumEv] = {};
     bool have_times = false;
-    bool sorted_in_profiled_step = false;
+    bool prof_sorted = false, prof_prologue = false;
 
     bool use_graph = true;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer parity][tiled]
 
     std::string err;
 };
@@ -112,7 +125,10 @@ ParticleArrays& state(cosmos_pm* h) { return h->buf[h->cur]; }
 
 int sort_now(cosmos_pm* h);
 
-// One step's kernels on stream st, for the buffer parity `cur`.
+// One step's kernels on stream st (buffer parity `cur`), assuming rho holds the
+// density of the current positions:
+//   FFT convolution rho -> phi, gradient phi -> force, clear rho,
+//   fused gather + update + deposit of the new positions into rho.
 int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     ParticleArrays& p = state(h);
     const size_t NN = size_t(h->N) * h->N;
@@ -120,22 +136,38 @@ int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[i], st));
         return COSMOS_OK;
     };
-    CPM_TRY(rec(kStDeposit));
-    CPM_CUDA(cudaMemsetAsync(h->rho, 0, NN * sizeof(float), st));
-    CPM_CUDA(cpm::launch_deposit_global(p, h->P, h->rho, h->N, h->cic, h->nsm, st));
-    CPM_TRY(rec(kStRows));
+    CPM_TRY(rec(kEvFft));
     CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
-    // the three FFT passes are timed together (rows, cols, inverse rows)
-    CPM_TRY(rec(kStForce));
+    CPM_TRY(rec(kEvForce));
     CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
-    CPM_TRY(rec(kStIntegrate));
-    CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
-    CPM_TRY(rec(kStSort));
+    CPM_TRY(rec(kEvFused));
+    CPM_CUDA(cudaMemsetAsync(h->rho, 0, NN * sizeof(float), st));
+    if (h->items_valid)
+        CPM_CUDA(cpm::launch_fused_tiles(h->items, h->n_items, p, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->gran,
+                                         h->tiles_grid, st));
+    else
+        CPM_CUDA(cpm::launch_fused_global(p, h->P, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->nsm, st));
+    CPM_TRY(rec(kEvEnd));
     return COSMOS_OK;
 }
 
+// Density of the current positions (first step after the state was written).
+int enqueue_prologue(cosmos_pm* h, cudaStream_t st) {
+    CPM_CUDA(cudaMemsetAsync(h->rho, 0, size_t(h->N) * h->N * sizeof(float), st));
+    CPM_CUDA(cpm::launch_deposit_global(state(h), h->P, h->rho, h->N, h->cic, h->nsm, st));
+    h->density_valid = true;
+    return COSMOS_OK;
+}
+
+// Invalidate what depends on the particle state after a host-side rewrite.
+void state_rewritten(cosmos_pm* h) {
+    h->sort_due = true;
+    h->items_valid = false;
+    h->density_valid = false;
+}
+
 int get_graph(cosmos_pm* h, cudaGraphExec_t* out) {
-    cudaGraphExec_t& g = h->graph[h->cur];
+    cudaGraphExec_t& g = h->graph[h->cur][h->items_valid ? 1 : 0];
     if (!g) {
         cudaGraph_t graph = nullptr;
         CPM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -158,16 +190,22 @@ int get_graph(cosmos_pm* h, cudaGraphExec_t* out) {
 }
 
 int enqueue_step(cosmos_pm* h) {
-    bool sorted = false;
+    bool sorted = false, prologue = false;
+    if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kEvPrologue], h->stream));
+    if (!h->density_valid) {
+        CPM_TRY(enqueue_prologue(h, h->stream));
+        prologue = true;
+    }
+    if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kEvSort], h->stream));
     if (h->sort_interval > 0 && (h->sort_due || h->steps_since_sort >= h->sort_interval)) {
-        if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kNumStages], h->stream));
         CPM_TRY(sort_now(h));
         sorted = true;
     }
     if (h->profiling) {
         CPM_TRY(enqueue_step_body(h, h->stream, true));
         h->have_times = true;
-        h->sorted_in_profiled_step = sorted;
+        h->prof_sorted = sorted;
+        h->prof_prologue = prologue;
     } else if (h->use_graph) {
         cudaGraphExec_t g = nullptr;
         CPM_TRY(get_graph(h, &g));
@@ -193,11 +231,14 @@ int sort_now(cosmos_pm* h) {
         CPM_CUDA(cudaMemcpyAsync(h->rs.vals[which] + h->Pq, h->rs.vals[0] + h->Pq, (h->P - h->Pq) * sizeof(uint32_t),
                                  cudaMemcpyDeviceToDevice, st));
     CPM_CUDA(cpm::launch_permute(src, dst, h->rs.vals[which], h->P, st));
+    CPM_CUDA(cpm::launch_build_items(h->rs.keys[which], dst.m, h->Pq, h->N, h->gran, h->tstart, h->tend, h->items,
+                                     h->n_items, h->max_items, st));
     h->cur ^= 1;
     h->identity_order = false;
     h->pos_valid = false;
     h->steps_since_sort = 0;
     h->sort_due = false;
+    h->items_valid = true;
     return COSMOS_OK;
 }
 
@@ -216,10 +257,12 @@ int check_range(cosmos_pm* h, int64_t count, int64_t offset) {
     return COSMOS_OK;
 }
 
+// Tile order pays off when a tile holds enough particles to amortise its
+// window staging: sort every 8 steps when the mean occupancy of the
+// 32x32-cell tiles is at least 256 particles.
 int default_sort_interval(int64_t P, int N) {
-    (void)P;
-    (void)N;
-    return 0;  // the global-atomic kernels do not use the tile order
+    const double tiles = double(N / 32 > 0 ? N / 32 : 1) * double(N / 32 > 0 ? N / 32 : 1);
+    return double(P) / tiles >= 256.0 ? 8 : 0;
 }
 
 void destroy_all(cosmos_pm* h) {
@@ -249,9 +292,14 @@ void destroy_all(cosmos_pm* h) {
         cudaFree(h->stage[i][1]);
         if (h->stage_ready[i]) cudaEventDestroy(h->stage_ready[i]);
         if (h->stage_done[i]) cudaEventDestroy(h->stage_done[i]);
-        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+        for (int j = 0; j < 2; ++j)
+            if (h->graph[i][j]) cudaGraphExecDestroy(h->graph[i][j]);
     }
     cudaFree(h->rs.counts);
+    cudaFree(h->tstart);
+    cudaFree(h->tend);
+    cudaFree(h->items);
+    cudaFree(h->n_items);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     for (auto& t : h->tickets) cudaEventDestroy(t.second);
@@ -274,8 +322,9 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return cpm::fail(COSMOS_ERR_INVALID, "dt and gravity_multiplier must be finite");
     if (cfg->force_mode != COSMOS_FORCE_GRADIENT)
         return cpm::fail(COSMOS_ERR_INVALID, "force_mode: only COSMOS_FORCE_GRADIENT is available");
-    if (cfg->sort_granularity > 13 || (cfg->sort_granularity >= 0 && (N >> cfg->sort_granularity) < 1))
-        return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity out of range");
+    if (cfg->sort_granularity != -1 &&
+        (cfg->sort_granularity < 4 || cfg->sort_granularity > 6 || (N >> cfg->sort_granularity) < 1))
+        return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity must be -1 (default) or 4..6 with 2^g <= N");
     int ndev = 0;
     CPM_CUDA(cudaGetDeviceCount(&ndev));
     if (cfg->device < 0 || cfg->device >= ndev) return cpm::fail(COSMOS_ERR_INVALID, "device ordinal out of range");
@@ -290,7 +339,7 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
     h->Pq = (h->P / 4) * 4;
     h->Palloc = ((h->P + 3) / 4) * 4;
     h->use_graph = cfg->use_graph != 0;
-    h->gran = cfg->sort_granularity >= 0 ? cfg->sort_granularity : (N >= 64 ? 5 : 2);
+    h->gran = cfg->sort_granularity >= 0 ? cfg->sort_granularity : (N >= 64 ? 5 : 4);
     {
         const int T = N >> h->gran;
         h->sort_bits = 2 * cpm::ilog2(T) + 1;
@@ -335,7 +384,18 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
             (rc = dalloc(&h->rs.counts, cpm::radix_counts_elems(h->rs.grid))))
             ;
     }
+    const int ntiles = (N >> h->gran) * (N >> h->gran);
+    h->max_items = cpm::max_work_items(h->Pq, ntiles);
+    if (rc == COSMOS_OK) {
+        if ((rc = dalloc(&h->tstart, size_t(ntiles))) || (rc = dalloc(&h->tend, size_t(ntiles))) ||
+            (rc = dalloc(&h->items, h->max_items)) || (rc = dalloc(&h->n_items, 1)))
+            ;
+    }
     if (rc != COSMOS_OK) return bail(rc);
+    if (cudaMemsetAsync(h->n_items, 0, sizeof(uint32_t), h->stream) != cudaSuccess)
+        return bail(cpm::fail(COSMOS_ERR_CUDA, "memset"));
+    if (cpm::prepare_tile_kernels(h->gran, h->cic, h->nsm, &h->tiles_grid) != cudaSuccess)
+        return bail(cpm::fail(COSMOS_ERR_CUDA, "tile kernel attributes"));
     // zero state; identities; filter
     for (int b = 0; b < 2; ++b) {
         ParticleArrays& a = h->buf[b];
@@ -383,7 +443,7 @@ int set_particles_impl(cosmos_pm* h, const float* x, const float* y, const float
         CPM_CUDA(cudaFreeAsync(tmp, st));
     }
     CPM_CUDA(cudaStreamSynchronize(st));
-    h->sort_due = true;
+    state_rewritten(h);
     return COSMOS_OK;
 }
 
@@ -538,7 +598,7 @@ int cosmos_pm_clear(cosmos_pm* h) {
         ParticleArrays& p = state(h);
         for (float* f : {p.x, p.y, p.xo, p.yo}) CPM_CUDA(cpm::launch_fill(f, -10.0f, h->P, h->stream));
         CPM_CUDA(cudaStreamSynchronize(h->stream));
-        h->sort_due = true;
+        state_rewritten(h);
         return COSMOS_OK;
     };
     return finish(h, impl());
@@ -595,6 +655,7 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
             case COSMOS_STAGE_DEPOSIT:
                 CPM_CUDA(cudaMemsetAsync(h->rho, 0, size_t(h->N) * h->N * sizeof(float), st));
                 CPM_CUDA(cpm::launch_deposit_global(p, h->P, h->rho, h->N, h->cic, h->nsm, st));
+                h->density_valid = true;
                 break;
             case COSMOS_STAGE_POTENTIAL:
                 CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
@@ -604,6 +665,7 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
                 break;
             case COSMOS_STAGE_INTEGRATE:
                 CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
+                h->density_valid = false;  // positions moved; the density is stale
                 break;
             default:
                 return cpm::fail(COSMOS_ERR_INVALID, "unknown stage");
@@ -645,6 +707,7 @@ int cosmos_pm_set_field(cosmos_pm* h, int32_t field, const float* host) {
         else return cpm::fail(COSMOS_ERR_INVALID, "unknown field");
         CPM_CUDA(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, h->stream));
         CPM_CUDA(cudaStreamSynchronize(h->stream));
+        if (field == COSMOS_FIELD_DENSITY) h->density_valid = true;  // the caller supplies the density
         return COSMOS_OK;
     };
     return finish(h, impl());
@@ -724,15 +787,15 @@ int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n) {
     DeviceGuard g(h->device);
     auto impl = [&]() -> int {
         if (!h->have_times) return cpm::fail(COSMOS_ERR_STATE, "no profiled step yet");
-        CPM_CUDA(cudaEventSynchronize(h->ev[kStSort]));
-        // entries: deposit, fft (all three passes), -, -, force, integrate, sort
-        float t[kNumStages] = {0};
-        CPM_CUDA(cudaEventElapsedTime(&t[0], h->ev[kStDeposit], h->ev[kStRows]));
-        CPM_CUDA(cudaEventElapsedTime(&t[1], h->ev[kStRows], h->ev[kStForce]));
-        CPM_CUDA(cudaEventElapsedTime(&t[4], h->ev[kStForce], h->ev[kStIntegrate]));
-        CPM_CUDA(cudaEventElapsedTime(&t[5], h->ev[kStIntegrate], h->ev[kStSort]));
-        if (h->sorted_in_profiled_step) CPM_CUDA(cudaEventElapsedTime(&t[6], h->ev[kNumStages], h->ev[kStDeposit]));
-        const int cnt = *n < kNumStages ? *n : kNumStages;
+        CPM_CUDA(cudaEventSynchronize(h->ev[kEvEnd]));
+        // entries: prologue deposit, fft convolution (3 passes), force, fused step, sort
+        float t[kNumTimes] = {0};
+        if (h->prof_prologue) CPM_CUDA(cudaEventElapsedTime(&t[kTPrologue], h->ev[kEvPrologue], h->ev[kEvSort]));
+        if (h->prof_sorted) CPM_CUDA(cudaEventElapsedTime(&t[kTSort], h->ev[kEvSort], h->ev[kEvFft]));
+        CPM_CUDA(cudaEventElapsedTime(&t[kTFft], h->ev[kEvFft], h->ev[kEvForce]));
+        CPM_CUDA(cudaEventElapsedTime(&t[kTForce], h->ev[kEvForce], h->ev[kEvFused]));
+        CPM_CUDA(cudaEventElapsedTime(&t[kTFused], h->ev[kEvFused], h->ev[kEvEnd]));
+        const int cnt = *n < kNumTimes ? *n : kNumTimes;
         for (int i = 0; i < cnt; ++i) times[i] = t[i];
         *n = cnt;
         return COSMOS_OK;
@@ -748,8 +811,8 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream) {
 
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
     if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
-    // deposit + FFT passes + gradient + integrate (the density clear is a memset node)
-    *launches = 1 + cpm::conv_launches_per_step() + 1 + 1;
+    // FFT passes + gradient + fused step kernel (the density clear is a memset node)
+    *launches = cpm::conv_launches_per_step() + 1 + 1;
     return COSMOS_OK;
 }
 

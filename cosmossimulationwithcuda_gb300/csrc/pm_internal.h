@@ -63,4 +63,30 @@ cudaError_t launch_fill(float* v, float value, int64_t n, cudaStream_t st);
 cudaError_t launch_diagnostics(const ParticleArrays& p, int64_t P, const float* phi, int N, float dt, double* out,
                                cudaStream_t st);
 
+// pm_tiles.cu -- tile-ordered fused gather + update + next-step deposit
+constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's window
+constexpr int kItemMax = 4096;  // particles per work item
+constexpr int kItemDirect = 256; // items with fewer particles skip the shared windows
+struct WorkItem {
+    int x0, y0;           // window origin (cells): tile origin - kTileHalo
+    uint32_t begin, end;  // slot range
+    float scale;          // fixed-point scale of the deposit window (a power of two)
+    float inv_scale;      // 1 / scale
+    float heavy;          // particles heavier than this deposit with global float atomics
+    uint32_t pad;
+};
+size_t tile_window_smem(int gran);
+size_t max_work_items(int64_t Pq, int ntiles);
+cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid);
+// Builds the work items of the sorted state and their deposit scales (the
+// masses of the sorted particles are read from `m`).
+cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
+                               uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
+                               cudaStream_t st);
+cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
+                               const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
+                               cudaStream_t st);
+cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
+                                float dt, int nsm, cudaStream_t st);
+
 }  // namespace cpm

@@ -12,6 +12,7 @@
 //    x' > N-2 -> -(N-4), xOld' = pre-step x (unwrapped) (:286-303).
 #include "pm_common.cuh"
 #include "pm_internal.h"
+#include "pm_particle_math.cuh"
 
 namespace cpm {
 
@@ -112,32 +113,14 @@ __device__ __forceinline__ void gather_update(const float2* __restrict__ force, 
     const int cx = int(px), cy = int(py);
     if (!active_cell(cx, cy, N)) return;
     const size_t c = size_t(cx) + size_t(cy) * N;
-    float Fx, Fy;
+    float2 F;
     if (cic) {
-        const float fx = __fsub_rn(px, float(cx)), fy = __fsub_rn(py, float(cy));
-        const float x1 = __fsub_rn(1.0f, fx), y1 = __fsub_rn(1.0f, fy);
-        const float w00 = __fmul_rn(x1, y1), w10 = __fmul_rn(fx, y1);
-        const float w01 = __fmul_rn(x1, fy), w11 = __fmul_rn(fx, fy);
-        const float2 f00 = __ldg(force + c), f10 = __ldg(force + c + 1);
-        const float2 f01 = __ldg(force + c + N), f11 = __ldg(force + c + N + 1);
-        Fx = __fmaf_rn(f11.x, w11, __fmaf_rn(f01.x, w01, __fmaf_rn(f10.x, w10, __fmul_rn(f00.x, w00))));
-        Fy = __fmaf_rn(f11.y, w11, __fmaf_rn(f01.y, w01, __fmaf_rn(f10.y, w10, __fmul_rn(f00.y, w00))));
+        const CicWeights w = cic_weights(px, py, cx, cy);
+        F = bilinear(w, __ldg(force + c), __ldg(force + c + 1), __ldg(force + c + N), __ldg(force + c + N + 1));
     } else {
-        const float2 f = __ldg(force + c);
-        Fx = f.x;
-        Fy = f.y;
+        F = __ldg(force + c);
     }
-    float nx = __fmaf_rn(__fmul_rn(dt, Fx), dt, __fmaf_rn(2.0f, px, -pxo));
-    float ny = __fmaf_rn(__fmul_rn(dt, Fy), dt, __fmaf_rn(2.0f, py, -pyo));
-    const float span = float(N) - 4.0f, hi = float(N) - 2.0f;
-    if (nx < 2.0f) nx = __fadd_rn(nx, span);
-    if (ny < 2.0f) ny = __fadd_rn(ny, span);
-    if (nx > hi) nx = __fsub_rn(nx, span);
-    if (ny > hi) ny = __fsub_rn(ny, span);
-    pxo = px;
-    pyo = py;
-    px = nx;
-    py = ny;
+    verlet_wrap(px, py, pxo, pyo, F, dt, N);
 }
 
 __global__ void __launch_bounds__(kThreads) k_integrate(const float2* __restrict__ force, float4* __restrict__ x,
@@ -203,7 +186,8 @@ int radix_grid(int64_t n, int nsm) {
     return int(g);
 }
 
-size_t radix_counts_elems(int grid) { return size_t(256) * grid; }
+// counts[256][grid] followed by the 256 digit totals
+size_t radix_counts_elems(int grid) { return size_t(256) * grid + 256; }
 
 __global__ void __launch_bounds__(kRsThreads) k_radix_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
                                                               int64_t tiles_per_cta, uint32_t* __restrict__ counts) {
@@ -218,39 +202,65 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_upsweep(const uint32_t* __
     counts[size_t(threadIdx.x) * gridDim.x + blockIdx.x] = hist[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* __restrict__ counts, int total) {
-    __shared__ uint32_t part[1024];
-    const int seg = (total + 1023) / 1024;
-    const int lo = threadIdx.x * seg;
-    const int hi = min(lo + seg, total);
-    uint32_t s = 0;
-    for (int i = lo; i < hi; ++i) s += counts[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+// Block-wide exclusive scan of one value per thread (256 threads); *total gets the sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += n;
     }
-    uint32_t run = part[threadIdx.x] - s;  // exclusive
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0, all = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t s = warp_sums[i];
+        wbase += i < w ? s : 0u;
+        all += s;
+    }
+    __syncthreads();
+    *total = all;
+    return wbase + incl - v;
+}
+
+// Row scan: CTA d scans counts[d][0..G) in place (exclusive) and writes the row
+// total to digit_total[d].  The digit prefix is added in the downsweep.
+__global__ void __launch_bounds__(kRsThreads) k_radix_scan_rows(uint32_t* __restrict__ counts, int G,
+                                                                uint32_t* __restrict__ digit_total) {
+    uint32_t* row = counts + size_t(blockIdx.x) * G;
+    const int per = (G + kRsThreads - 1) / kRsThreads;
+    const int lo = threadIdx.x * per;
+    const int hi = min(lo + per, G);
+    uint32_t s = 0;
+    for (int i = lo; i < hi; ++i) s += row[i];
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan_256(s, &tot);
     for (int i = lo; i < hi; ++i) {
-        const uint32_t c = counts[i];
-        counts[i] = run;
+        const uint32_t c = row[i];
+        row[i] = run;
         run += c;
     }
+    if (threadIdx.x == 0) digit_total[blockIdx.x] = tot;
 }
 
 __global__ void __launch_bounds__(kRsThreads) k_radix_downsweep(const uint32_t* __restrict__ kin,
                                                                 const uint32_t* __restrict__ vin,
                                                                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                                 int64_t n, int shift, int64_t tiles_per_cta,
-                                                                const uint32_t* __restrict__ counts) {
+                                                                const uint32_t* __restrict__ counts,
+                                                                const uint32_t* __restrict__ digit_total) {
     __shared__ uint32_t run_off[256];
     __shared__ uint32_t tile_total[256];
     __shared__ uint32_t wcnt[kRsWarps][256];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    run_off[tid] = counts[size_t(tid) * gridDim.x + blockIdx.x];
+    {
+        uint32_t all;
+        const uint32_t digit_base = block_exclusive_scan_256(digit_total[tid], &all);
+        run_off[tid] = digit_base + counts[size_t(tid) * gridDim.x + blockIdx.x];
+    }
     const uint32_t lt_mask = (1u << lane) - 1u;
     const int64_t t0 = int64_t(blockIdx.x) * tiles_per_cta;
     for (int64_t t = 0; t < tiles_per_cta; ++t) {
@@ -310,11 +320,12 @@ cudaError_t launch_radix_sort(RadixScratch& s, int64_t n, int bits, int* result_
     }
     const int64_t tiles = (n + kRsTile - 1) / kRsTile;
     const int64_t tpc = (tiles + s.grid - 1) / s.grid;
+    uint32_t* digit_total = s.counts + size_t(256) * s.grid;
     for (int shift = 0; shift < bits; shift += 8) {
         k_radix_upsweep<<<s.grid, kRsThreads, 0, st>>>(s.keys[cur], n, shift, tpc, s.counts);
-        k_radix_scan<<<1, 1024, 0, st>>>(s.counts, int(radix_counts_elems(s.grid)));
+        k_radix_scan_rows<<<256, kRsThreads, 0, st>>>(s.counts, s.grid, digit_total);
         k_radix_downsweep<<<s.grid, kRsThreads, 0, st>>>(s.keys[cur], s.vals[cur], s.keys[cur ^ 1], s.vals[cur ^ 1], n,
-                                                        shift, tpc, s.counts);
+                                                        shift, tpc, s.counts, digit_total);
         cur ^= 1;
     }
     *result_buf = cur;

@@ -1,0 +1,407 @@
+// Tile-ordered particle kernels: the fused gather + update + next-step deposit.
+//
+// After a sort the particle state is ordered by the Morton code of its
+// (2^GRAN)^2-cell tile.  Each tile's slot range is cut into work items of at
+// most kItemMax particles.  A CTA takes one item at a time and
+//   1. stages the force field of the tile plus a kTileHalo-cell border (+1 for
+//      the CIC corners) into shared memory,
+//   2. streams the item's particles with 128-bit loads (x, y, xOld, yOld, m),
+//      gathers the force from the window, applies the position-Verlet update
+//      and wrap of the reference, and stores the new state,
+//   3. deposits the NEW positions (the next step's density) into a shared
+//      window of 32-bit fixed-point accumulators with native integer atomics,
+//   4. flushes the window once into the global density with 16-byte vector
+//      float reductions, skipping empty 4-cell groups.
+// Particles that drifted outside the window since the last sort fall back to
+// global loads / float atomics, so the result is correct for any drift.
+// Items with fewer than kItemDirect particles (sparse tiles) skip the windows.
+//
+// Fixed point: an item's deposits are scaled by S = 2^k <= 2^30 / M, M the
+// summed mass of the item's (non-heavy) particles, so no window cell can
+// overflow; S is a power of two, so unit masses stay exact and the flush
+// scales back exactly.  Particles heavier than M/128 deposit with global float
+// atomics so that one heavy body cannot coarsen the resolution of the others.
+// (Shared-memory float atomicAdd is a compare-and-swap loop on this
+// architecture; integer atomicAdd is a single native operation.)
+//
+// Fusing step n's integrate with step n+1's deposit reads each particle once
+// per step (20 B) and writes it once (16 B) instead of 12 + 32 B in two
+// kernels; the reference does the deposit (CosmosCuda.cuh:446-595) and the
+// gather (:231-312) as separate passes.
+#include <cfloat>
+
+#include "pm_common.cuh"
+#include "pm_internal.h"
+#include "pm_particle_math.cuh"
+
+namespace cpm {
+
+namespace {
+
+constexpr int kFusedThreads = 256;
+
+__host__ __device__ constexpr int win_y(int gran) { return (1 << gran) + 2 * kTileHalo + 1; }
+__host__ __device__ constexpr int win_x(int gran) { return (win_y(gran) + 3) & ~3; }
+
+__device__ __forceinline__ uint32_t compact_bits(uint32_t v) {
+    v &= 0x55555555u;
+    v = (v | (v >> 1)) & 0x33333333u;
+    v = (v | (v >> 2)) & 0x0F0F0F0Fu;
+    v = (v | (v >> 4)) & 0x00FF00FFu;
+    v = (v | (v >> 8)) & 0x0000FFFFu;
+    return v;
+}
+
+struct Window {
+    const float2* f;  // staged force (nullptr: read the global field)
+    uint32_t* d;      // fixed-point deposit window (nullptr: global float atomics)
+    int x0, y0;
+    float scale, heavy;
+};
+
+__device__ __forceinline__ void deposit_global(float* __restrict__ rho, int N, int nx, int ny, float a, float b,
+                                               float c, float d, bool cic) {
+    float* g = rho + size_t(nx) + size_t(ny) * N;
+    if (cic) {
+        atomicAdd(g, a);
+        atomicAdd(g + 1, b);
+        atomicAdd(g + N, c);
+        atomicAdd(g + N + 1, d);
+    } else {
+        atomicAdd(g, a);
+    }
+}
+
+// One particle: gather, update, deposit of the new position.
+template <int CIC, int WX, int WY>
+__device__ __forceinline__ void step_particle(float& px, float& py, float& pxo, float& pyo, float pm, const Window& w,
+                                              const float2* __restrict__ force, float* __restrict__ rho, int N,
+                                              float dt) {
+    const int cx = int(px), cy = int(py);
+    if (!active_cell(cx, cy, N)) return;
+    const int lx = cx - w.x0, ly = cy - w.y0;
+    float2 F;
+    if (CIC) {
+        const CicWeights cw = cic_weights(px, py, cx, cy);
+        if (w.f && unsigned(lx) < unsigned(WX - 1) && unsigned(ly) < unsigned(WY - 1)) {
+            const float2* f = w.f + ly * WX + lx;
+            F = bilinear(cw, f[0], f[1], f[WX], f[WX + 1]);
+        } else {
+            const size_t c = size_t(cx) + size_t(cy) * N;
+            F = bilinear(cw, __ldg(force + c), __ldg(force + c + 1), __ldg(force + c + N), __ldg(force + c + N + 1));
+        }
+    } else {
+        F = (w.f && unsigned(lx) < unsigned(WX) && unsigned(ly) < unsigned(WY))
+                ? w.f[ly * WX + lx]
+                : __ldg(force + size_t(cx) + size_t(cy) * N);
+    }
+    verlet_wrap(px, py, pxo, pyo, F, dt, N);
+    const int nx = int(px), ny = int(py);
+    if (!active_cell(nx, ny, N)) return;
+    const int mx = nx - w.x0, my = ny - w.y0;
+    if (CIC) {
+        const CicWeights cw = cic_weights(px, py, nx, ny);
+        const float a = __fmul_rn(cw.w00, pm), b = __fmul_rn(cw.w10, pm);
+        const float c = __fmul_rn(cw.w01, pm), d = __fmul_rn(cw.w11, pm);
+        if (w.d && pm <= w.heavy && unsigned(mx) < unsigned(WX - 1) && unsigned(my) < unsigned(WY - 1)) {
+            uint32_t* s = w.d + my * WX + mx;
+            atomicAdd(s, __float2uint_rn(a * w.scale));
+            atomicAdd(s + 1, __float2uint_rn(b * w.scale));
+            atomicAdd(s + WX, __float2uint_rn(c * w.scale));
+            atomicAdd(s + WX + 1, __float2uint_rn(d * w.scale));
+        } else {
+            deposit_global(rho, N, nx, ny, a, b, c, d, true);
+        }
+    } else {
+        if (w.d && pm <= w.heavy && unsigned(mx) < unsigned(WX) && unsigned(my) < unsigned(WY))
+            atomicAdd(w.d + my * WX + mx, __float2uint_rn(pm * w.scale));
+        else
+            deposit_global(rho, N, nx, ny, pm, 0.f, 0.f, 0.f, false);
+    }
+}
+
+template <int CIC, int WX, int WY>
+__device__ __forceinline__ void step_range(const ParticleArrays& p, uint32_t b, uint32_t e, const Window& w,
+                                           const float2* __restrict__ force, float* __restrict__ rho, int N,
+                                           float dt) {
+    const uint32_t b4 = (b + 3u) & ~3u, e4 = e & ~3u;
+    {  // ragged head / tail (or the whole range when it spans no full group)
+        const uint32_t h_end = b4 < e ? b4 : e;
+        const uint32_t t_beg = e4 > h_end ? e4 : h_end;
+        const uint32_t nh = h_end - b, nt = e - t_beg;
+        if (threadIdx.x < nh + nt) {
+            const uint32_t i = threadIdx.x < nh ? b + threadIdx.x : t_beg + (threadIdx.x - nh);
+            float px = p.x[i], py = p.y[i], pxo = p.xo[i], pyo = p.yo[i];
+            step_particle<CIC, WX, WY>(px, py, pxo, pyo, p.m[i], w, force, rho, N, dt);
+            p.x[i] = px;
+            p.y[i] = py;
+            p.xo[i] = pxo;
+            p.yo[i] = pyo;
+        }
+    }
+    if (b4 < e4) {
+        float4* X = reinterpret_cast<float4*>(p.x);
+        float4* Y = reinterpret_cast<float4*>(p.y);
+        float4* XO = reinterpret_cast<float4*>(p.xo);
+        float4* YO = reinterpret_cast<float4*>(p.yo);
+        const float4* Mm = reinterpret_cast<const float4*>(p.m);
+        for (uint32_t g = (b4 >> 2) + threadIdx.x; g < (e4 >> 2); g += kFusedThreads) {
+            float4 x = __ldcs(X + g), y = __ldcs(Y + g), xo = __ldcs(XO + g), yo = __ldcs(YO + g);
+            const float4 m = __ldcs(Mm + g);
+            step_particle<CIC, WX, WY>(x.x, y.x, xo.x, yo.x, m.x, w, force, rho, N, dt);
+            step_particle<CIC, WX, WY>(x.y, y.y, xo.y, yo.y, m.y, w, force, rho, N, dt);
+            step_particle<CIC, WX, WY>(x.z, y.z, xo.z, yo.z, m.z, w, force, rho, N, dt);
+            step_particle<CIC, WX, WY>(x.w, y.w, xo.w, yo.w, m.w, w, force, rho, N, dt);
+            __stcs(X + g, x);
+            __stcs(Y + g, y);
+            __stcs(XO + g, xo);
+            __stcs(YO + g, yo);
+        }
+    }
+}
+
+}  // namespace
+
+// ---- work items from the sorted keys -------------------------------------------------------
+__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, int64_t n, uint32_t ntiles,
+                              uint32_t* __restrict__ tstart, uint32_t* __restrict__ tend) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (k >= ntiles) continue;
+        if (i == 0 || keys[i - 1] != k) tstart[k] = uint32_t(i);
+        if (i == n - 1 || keys[i + 1] != k) tend[k] = uint32_t(i + 1);
+    }
+}
+
+// One CTA: count the items of each tile, scan, write the items (tile order).
+__global__ void __launch_bounds__(1024) k_build_items(const uint32_t* __restrict__ tstart,
+                                                      const uint32_t* __restrict__ tend, int ntiles, int gran,
+                                                      int item_max, WorkItem* __restrict__ items,
+                                                      uint32_t* __restrict__ n_items) {
+    __shared__ uint32_t part[1024];
+    const int seg = (ntiles + 1023) / 1024;
+    const int lo = int(threadIdx.x) * seg;
+    const int hi = min(lo + seg, ntiles);
+    uint32_t cnt = 0;
+    for (int t = lo; t < hi; ++t) cnt += (tend[t] - tstart[t] + item_max - 1) / item_max;
+    part[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t base = part[threadIdx.x] - cnt;
+    for (int t = lo; t < hi; ++t) {
+        const uint32_t s = tstart[t], c = tend[t] - s;
+        const uint32_t nch = (c + item_max - 1) / item_max;
+        const int x0 = int(compact_bits(uint32_t(t)) << gran) - kTileHalo;
+        const int y0 = int(compact_bits(uint32_t(t) >> 1) << gran) - kTileHalo;
+        for (uint32_t j = 0; j < nch; ++j) {
+            WorkItem w;
+            w.x0 = x0;
+            w.y0 = y0;
+            w.begin = s + uint32_t((uint64_t(c) * j) / nch);
+            w.end = s + uint32_t((uint64_t(c) * (j + 1)) / nch);
+            w.scale = 1.0f;
+            w.inv_scale = 1.0f;
+            w.heavy = FLT_MAX;
+            w.pad = 0;
+            items[base++] = w;
+        }
+    }
+    if (threadIdx.x == 1023) *n_items = part[1023];
+}
+
+__device__ __forceinline__ float block_sum_256(float v, float* red) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += red[i];
+    return s;
+}
+
+// Deposit scale of each item: S = 2^k <= 2^30 / M_light, with M_light the mass
+// of the item's particles no heavier than 1/128 of the item's total mass.
+__global__ void __launch_bounds__(256) k_item_scales(const float* __restrict__ m, WorkItem* __restrict__ items,
+                                                     const uint32_t* __restrict__ n_items) {
+    __shared__ float red[8];
+    const uint32_t it = blockIdx.x;
+    if (it >= *n_items) return;
+    const uint32_t b = items[it].begin, e = items[it].end;
+    float s = 0.0f;
+    for (uint32_t i = b + threadIdx.x; i < e; i += 256) s += __ldg(m + i);
+    const float total = block_sum_256(s, red);
+    const float heavy = total / 128.0f;
+    float sl = 0.0f;
+    for (uint32_t i = b + threadIdx.x; i < e; i += 256) {
+        const float mi = __ldg(m + i);
+        sl += mi <= heavy ? mi : 0.0f;
+    }
+    const float light = block_sum_256(sl, red);
+    if (threadIdx.x == 0) {
+        int ex = 30;
+        if (light > 0.0f) {
+            int e2;
+            frexpf(light * 1.001f, &e2);  // light < 2^e2
+            ex = 30 - e2;
+        }
+        ex = ex > 120 ? 120 : (ex < -120 ? -120 : ex);
+        items[it].scale = ldexpf(1.0f, ex);
+        items[it].inv_scale = ldexpf(1.0f, -ex);
+        items[it].heavy = heavy;
+    }
+}
+
+// ---- the fused step kernel, tile windows ----------------------------------------------------
+template <int CIC, int GRAN>
+__global__ void __launch_bounds__(kFusedThreads) k_fused_tiles(const WorkItem* __restrict__ items,
+                                                               const uint32_t* __restrict__ n_items_p,
+                                                               ParticleArrays p, const float2* __restrict__ force,
+                                                               float* __restrict__ rho, int N, float dt) {
+    constexpr int WY = win_y(GRAN), WX = win_x(GRAN);
+    extern __shared__ float4 smem4[];
+    float2* fwin = reinterpret_cast<float2*>(smem4);
+    uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
+    const uint32_t n_items = *n_items_p;
+    for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const WorkItem item = items[it];
+        if (item.end - item.begin < uint32_t(kItemDirect)) {
+            // sparse tile: no windows, global gathers and atomics
+            const Window w{nullptr, nullptr, item.x0, item.y0, 1.0f, 0.0f};
+            step_range<CIC, WX, WY>(p, item.begin, item.end, w, force, rho, N, dt);
+            continue;
+        }
+        for (int i = threadIdx.x; i < WY * WX; i += kFusedThreads) {
+            const int r = i / WX, c = i - r * WX;
+            const int gx = item.x0 + c, gy = item.y0 + r;
+            float2 f = make_float2(0.0f, 0.0f);
+            if (gx >= 0 && gx < N && gy >= 0 && gy < N) f = __ldg(force + size_t(gy) * N + gx);
+            fwin[i] = f;
+            dwin[i] = 0u;
+        }
+        __syncthreads();
+        const Window w{fwin, dwin, item.x0, item.y0, item.scale, item.heavy};
+        step_range<CIC, WX, WY>(p, item.begin, item.end, w, force, rho, N, dt);
+        __syncthreads();
+        constexpr int W4 = WX / 4;
+        const uint4* d4 = reinterpret_cast<const uint4*>(dwin);
+        const float inv = item.inv_scale;
+        for (int i = threadIdx.x; i < WY * W4; i += kFusedThreads) {
+            const int r = i / W4, c4 = i - r * W4;
+            const int gy = item.y0 + r, gx = item.x0 + 4 * c4;
+            if (gy < 0 || gy >= N || gx < 0 || gx >= N) continue;
+            const uint4 q = d4[i];
+            if ((q.x | q.y | q.z | q.w) != 0u)
+                red_add_v4(rho + size_t(gy) * N + gx,
+                           make_float4(__uint2float_rn(q.x) * inv, __uint2float_rn(q.y) * inv,
+                                       __uint2float_rn(q.z) * inv, __uint2float_rn(q.w) * inv));
+        }
+        __syncthreads();
+    }
+}
+
+// ---- the fused step kernel, no tile order (global gathers and atomics) -----------------------
+template <int CIC>
+__global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p, int64_t ngroups,
+                                                                const float2* __restrict__ force,
+                                                                float* __restrict__ rho, int N, float dt) {
+    float4* X = reinterpret_cast<float4*>(p.x);
+    float4* Y = reinterpret_cast<float4*>(p.y);
+    float4* XO = reinterpret_cast<float4*>(p.xo);
+    float4* YO = reinterpret_cast<float4*>(p.yo);
+    const float4* Mm = reinterpret_cast<const float4*>(p.m);
+    const Window w{nullptr, nullptr, 0, 0, 1.0f, 0.0f};
+    for (int64_t g = blockIdx.x * int64_t(kFusedThreads) + threadIdx.x; g < ngroups;
+         g += int64_t(gridDim.x) * kFusedThreads) {
+        float4 x = __ldcs(X + g), y = __ldcs(Y + g), xo = __ldcs(XO + g), yo = __ldcs(YO + g);
+        const float4 m = __ldcs(Mm + g);
+        step_particle<CIC, 4, 4>(x.x, y.x, xo.x, yo.x, m.x, w, force, rho, N, dt);
+        step_particle<CIC, 4, 4>(x.y, y.y, xo.y, yo.y, m.y, w, force, rho, N, dt);
+        step_particle<CIC, 4, 4>(x.z, y.z, xo.z, yo.z, m.z, w, force, rho, N, dt);
+        step_particle<CIC, 4, 4>(x.w, y.w, xo.w, yo.w, m.w, w, force, rho, N, dt);
+        __stcs(X + g, x);
+        __stcs(Y + g, y);
+        __stcs(XO + g, xo);
+        __stcs(YO + g, yo);
+    }
+}
+
+// ---- host side -------------------------------------------------------------------------------
+size_t tile_window_smem(int gran) { return size_t(win_y(gran)) * win_x(gran) * (sizeof(float2) + sizeof(uint32_t)); }
+
+size_t max_work_items(int64_t Pq, int ntiles) { return size_t(Pq / kItemMax) + size_t(ntiles) + 1; }
+
+template <int CIC, int GRAN>
+static cudaError_t prep_tiles() {
+    return cudaFuncSetAttribute(k_fused_tiles<CIC, GRAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(tile_window_smem(GRAN)));
+}
+
+cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid) {
+    cudaError_t e = cudaErrorInvalidValue;
+    int per_sm = 0;
+    const size_t smem = tile_window_smem(gran);
+#define CPM_TILES(C, G)                                                                                       \
+    if (cic == C && gran == G) {                                                                              \
+        e = prep_tiles<C, G>();                                                                               \
+        if (e == cudaSuccess)                                                                                 \
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tiles<C, G>, kFusedThreads, smem); \
+    }
+    CPM_TILES(0, 4) CPM_TILES(0, 5) CPM_TILES(0, 6) CPM_TILES(1, 4) CPM_TILES(1, 5) CPM_TILES(1, 6)
+#undef CPM_TILES
+    if (e == cudaSuccess) *grid = nsm * (per_sm > 0 ? per_sm : 1);
+    return e;
+}
+
+cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
+                               uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
+                               cudaStream_t st) {
+    const int t = N >> gran;
+    const uint32_t ntiles = uint32_t(t) * uint32_t(t);
+    cudaError_t e = cudaMemsetAsync(tstart, 0, ntiles * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(tend, 0, ntiles * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    if (Pq > 0) {
+        int64_t g = (Pq + 255) / 256;
+        if (g > 4096) g = 4096;
+        k_tile_ranges<<<int(g), 256, 0, st>>>(sorted_keys, Pq, ntiles, tstart, tend);
+    }
+    k_build_items<<<1, 1024, 0, st>>>(tstart, tend, int(ntiles), gran, kItemMax, items, n_items);
+    if (max_items > 0) k_item_scales<<<unsigned(max_items), 256, 0, st>>>(m, items, n_items);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
+                               const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
+                               cudaStream_t st) {
+    const size_t smem = tile_window_smem(gran);
+#define CPM_TILES(C, G)                                                                                      \
+    if (cic == C && gran == G) {                                                                             \
+        k_fused_tiles<C, G><<<grid, kFusedThreads, smem, st>>>(items, n_items, p, force, rho, N, dt);        \
+        return cudaGetLastError();                                                                           \
+    }
+    CPM_TILES(0, 4) CPM_TILES(0, 5) CPM_TILES(0, 6) CPM_TILES(1, 4) CPM_TILES(1, 5) CPM_TILES(1, 6)
+#undef CPM_TILES
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
+                                float dt, int nsm, cudaStream_t st) {
+    const int64_t ng = P / 4;
+    if (ng <= 0) return cudaGetLastError();
+    int64_t g = (ng + kFusedThreads - 1) / kFusedThreads;
+    const int64_t cap = int64_t(nsm) * 8;
+    if (g > cap) g = cap;
+    if (cic)
+        k_fused_global<1><<<int(g), kFusedThreads, 0, st>>>(p, ng, force, rho, N, dt);
+    else
+        k_fused_global<0><<<int(g), kFusedThreads, 0, st>>>(p, ng, force, rho, N, dt);
+    return cudaGetLastError();
+}
+
+}  // namespace cpm

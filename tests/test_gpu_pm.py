@@ -239,6 +239,50 @@ def test_sorted_and_unsorted_steps_identical_ngp(cosmos_lib):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("cic", [False, True])
+@pytest.mark.parametrize("sort_interval", [0, 1])
+def test_fused_step_deposits_new_positions(cosmos_lib, cic, sort_interval):
+    """After a step the density field holds the deposit of the NEW positions
+    (the fused kernel's next-step deposit), in both the tile and global paths."""
+    N, P, dt = 256, 300_000, 0.001
+    st = ics.exponential_disk(P, N, dt, seed=21, scale=30.0)
+    with _sim(cosmos_lib, N, P, cic, dt=dt, sort_interval=sort_interval) as s:
+        s.set_state(st)
+        s.step(3)
+        s.synchronize()
+        gx, gy, gxo, gyo, gm = s.get_particles()
+        rho = s.get_field(cosmos_lib.FIELD_DENSITY)
+    o = pm_oracle.OraclePM(N, cic, dt, 1.0, fp64=True)
+    o.deposit(gx, gy, gm)
+    assert rel_l2(rho, o.density()) < 1e-6
+
+
+def test_fused_step_large_drift_fallbacks(cosmos_lib):
+    """Fast particles leave their tile windows between sorts: the global
+    fallbacks of the fused kernel must keep the trajectory exact."""
+    N, P, dt = 256, 100_000, 0.01
+    rng = np.random.default_rng(3)
+    st = _random_state(rng, P, N, margin=20.0, vel=0.0)
+    v = rng.normal(0.0, 300.0, (2, P))  # ~3 cells per step
+    st.x_old[:] = st.x - (v[0] * dt).astype(np.float32)
+    st.y_old[:] = st.y - (v[1] * dt).astype(np.float32)
+    with _sim(cosmos_lib, N, P, True, dt=dt, sort_interval=1000) as s:
+        s.set_state(st)
+        s.step(6)
+        s.synchronize()
+        gx, gy, gxo, gyo, gm = s.get_particles()
+        rho = s.get_field(cosmos_lib.FIELD_DENSITY)
+    o = pm_oracle.OraclePM(N, True, dt, 1.0, fp64=True)
+    ref = st.copy()
+    o.step(ref.x, ref.y, ref.x_old, ref.y_old, ref.m, 6)
+    keep = _interior(st, N, 25.0) & _interior(ref, N, 3.0)
+    assert np.abs(gx - ref.x)[keep].max() <= 1e-3
+    assert np.abs(gy - ref.y)[keep].max() <= 1e-3
+    o2 = pm_oracle.OraclePM(N, True, dt, 1.0, fp64=True)
+    o2.deposit(gx, gy, gm)
+    assert rel_l2(rho, o2.density()) < 1e-6
+
+
 def test_positions_async_ordered_and_internal(cosmos_lib, rng):
     N, P = 256, 50_000
     st = _random_state(rng, P, N)
