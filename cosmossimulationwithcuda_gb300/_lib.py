@@ -29,7 +29,9 @@ EXPORTS = (
     "cosmos_pm_get_field", "cosmos_pm_set_field", "cosmos_pm_sort", "cosmos_pm_tile_keys",
     "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
+    "cosmos_tile_sort_noalloc",
 )
+NOALLOC_MAX_PARTICLES = 1 << 20
 
 
 class Config(ctypes.Structure):
@@ -95,6 +97,7 @@ def load(path: str | None = None):
         "cosmos_pm_launches_per_step": (ctypes.c_int, [_vp, ctypes.POINTER(i32)]),
         "cosmos_pm_last_error": (ctypes.c_char_p, [_vp]),
         "cosmos_pm_version": (ctypes.c_char_p, []),
+        "cosmos_tile_sort_noalloc": (ctypes.c_int, [_vp, _vp, i64, i32, i32, _vp, ctypes.c_uint64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -184,6 +184,25 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream);
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
 
+/* ---- tile sort without device allocation ---------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run (a host that owns a fixed device budget, code inside
+ * an allocator or memory-pool callback, a real-time loop where cudaMalloc may
+ * stall on a device-wide synchronisation): writes to perm_dev the stable sort
+ * permutation (perm[i] = index of the i-th particle in tile-key order, the
+ * keys of cosmos_pm_tile_keys) of n device-resident positions.  It calls no
+ * cudaMalloc / cudaFree: its scratch is a fixed device array of about 16.5 MB
+ * that every GPU loading this library keeps until the process exits, sized
+ * for COSMOS_NOALLOC_MAX_PARTICLES particles; larger n returns
+ * COSMOS_ERR_RANGE.  Work is enqueued on `stream` (a cudaStream_t as an
+ * integer, 0 = legacy default stream) and not waited for.  The first call on
+ * a device looks up the scratch address on that device: make it before any
+ * stream capture.  All calls on a device share the scratch, so calls whose
+ * work overlaps on the GPU race; serialise them. */
+#define COSMOS_NOALLOC_MAX_PARTICLES (1 << 20)
+int cosmos_tile_sort_noalloc(const float* x_dev, const float* y_dev, int64_t n, int32_t lattice_n,
+                             int32_t granularity, uint32_t* perm_dev, uint64_t stream);
+
 /* Message of the last error on this handle (or the last create failure when
  * h is NULL).  The string stays valid until the next call on the handle. */
 const char* cosmos_pm_last_error(cosmos_pm* h);
