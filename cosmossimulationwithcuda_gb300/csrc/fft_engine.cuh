@@ -115,13 +115,26 @@ __device__ __forceinline__ void fft_stage(const Load& load, const Store& store, 
 #pragma unroll
             for (int r = 0; r < R; ++r) v[q][r] = load(line, j + r * LR);
             if constexpr (Ns > 1) {
+                // one table load per butterfly (w^1); the other powers by complex
+                // multiplication in a tree of depth <= 3, so that a warp's twiddle
+                // reads stay close to coalesced
                 const int k = j % Ns;
                 constexpr int step = L / (Ns * R);
-#pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    C w = tw[(r * k * step) * tw_stride];
-                    if (DIR > 0) w.y = -w.y;
-                    v[q][r] = cmul(v[q][r], w);
+                C w1 = tw[(k * step) * tw_stride];
+                if (DIR > 0) w1.y = -w1.y;
+                v[q][1] = cmul(v[q][1], w1);
+                if constexpr (R >= 4) {
+                    const C w2 = cmul(w1, w1);
+                    const C w3 = cmul(w2, w1);
+                    v[q][2] = cmul(v[q][2], w2);
+                    v[q][3] = cmul(v[q][3], w3);
+                    if constexpr (R == 8) {
+                        const C w4 = cmul(w2, w2);
+                        v[q][4] = cmul(v[q][4], w4);
+                        v[q][5] = cmul(v[q][5], cmul(w4, w1));
+                        v[q][6] = cmul(v[q][6], cmul(w4, w2));
+                        v[q][7] = cmul(v[q][7], cmul(w4, w3));
+                    }
                 }
             }
             dft_r<R, DIR>(v[q]);

@@ -32,26 +32,39 @@
 namespace cpm {
 
 // ---- launch shapes ------------------------------------------------------------------
+// Launch shapes: about 4096 complex points per CTA (~35 KB of shared memory),
+// one radix-8 butterfly per thread per stage (so few registers per thread and
+// several CTAs per SM to hide the global-memory latency), and at least 4 rows
+// per CTA in the row passes so that the transposed spectrum moves in 32-byte
+// sectors.  FP64 (filter build) halves the rows to keep shared memory in range.
+constexpr int ceil_pow2_min(int v, int lo) { return v < lo ? lo : v; }
+
 template <class T, int N>
 struct RowShape {
     static constexpr int M = N / 2;
-    static constexpr int Bf = (N <= 256) ? 16 : (N <= 2048 ? 8 : 4);
-    static constexpr int B = (sizeof(T) == 8) ? (Bf / 2) : Bf;  // rows per CTA
-    static constexpr int NT = (N <= 64) ? 64 : (N <= 256 ? 128 : (N <= 4096 ? 256 : 512));
+    static constexpr int Bf0 = ceil_pow2_min(4096 / M, 4);
+    static constexpr int Bf = Bf0 > N ? N : Bf0;
+    static constexpr int B = (sizeof(T) == 8 && Bf > 1) ? (Bf / 2) : Bf;  // rows per CTA
+    static constexpr int NT0 = B * M / 8;
+    static constexpr int NT = NT0 < 64 ? 64 : (NT0 > 1024 ? 1024 : NT0);
+    static constexpr int MINB = NT <= 512 ? 2 : 1;
     static constexpr size_t smem = size_t(B) * LinePad<M>::value * sizeof(cplx_t<T>);
 };
 
 template <class T, int N>
 struct ColShape {
     static constexpr int M = N / 2;
-    static constexpr int B = (N <= 256) ? 8 : (N <= 512 ? 4 : (N <= 2048 ? 2 : 1));  // lines per CTA
-    static constexpr int NT = (N <= 128) ? 64 : (N <= 2048 ? 256 : 512);
+    static constexpr int B0 = ceil_pow2_min(4096 / N, 1);
+    static constexpr int B = B0 > M ? M : B0;  // lines per CTA
+    static constexpr int NT0 = B * N / 8;
+    static constexpr int NT = NT0 < 64 ? 64 : (NT0 > 1024 ? 1024 : NT0);
+    static constexpr int MINB = NT <= 512 ? 2 : 1;
     static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);
 };
 
 // ---- pass 1: rows, real -> half spectrum, transposed store --------------------------------
 template <class T, int N, int B, int NT>
-__global__ void __launch_bounds__(NT) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
+__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
                                                  const cplx_t<T>* __restrict__ tw) {
     using C = cplx_t<T>;
     constexpr int M = N / 2;
@@ -85,7 +98,7 @@ __global__ void __launch_bounds__(NT) k_rows_r2c(const T* __restrict__ in, cplx_
 // ---- pass 2: columns, forward FFT x K x inverse FFT ----------------------------------------
 // kq: (N/2+1) x (N/2+1) floats, kq[kx*(M+1) + min(ky, N-ky)].
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
+__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
                                                   const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;
@@ -127,7 +140,7 @@ __global__ void __launch_bounds__(NT) k_cols_conv(float2* __restrict__ spec, con
 // FP64 forward column FFT for the filter build: writes the real part of the
 // 2-D spectrum of a real, even input as ghat[kx][ky], kx in [0, N/2], ky in [0, N).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT) k_cols_fwd_real64(const double2* __restrict__ spec, double* __restrict__ ghat,
+__global__ void __launch_bounds__(NT, 1) k_cols_fwd_real64(const double2* __restrict__ spec, double* __restrict__ ghat,
                                                         const double2* __restrict__ tw) {
     using C = double2;
     constexpr int M = N / 2;
@@ -156,7 +169,7 @@ __global__ void __launch_bounds__(NT) k_cols_fwd_real64(const double2* __restric
 
 // ---- pass 3: rows, half spectrum (transposed) -> real potential rows -----------------------
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
+__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
                                                  const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;

@@ -46,6 +46,16 @@ __device__ __forceinline__ void verlet_wrap(float& px, float& py, float& pxo, fl
     py = ny;
 }
 
+// The reference's 4th-order difference (CosmosCuda.cuh:183-226) with the
+// operation order pinned: ((8r - rr) - 8l + ll) / 12 * g.  Out-of-range
+// neighbours (outside [0, N)) are replaced by the centre value by the caller.
+__device__ __forceinline__ float diff4(float ll, float l, float r, float rr, float g) {
+    float t = __fmaf_rn(8.0f, r, -rr);
+    t = __fmaf_rn(-8.0f, l, t);
+    t = __fadd_rn(t, ll);
+    return __fmul_rn(__fdiv_rn(t, 12.0f), g);
+}
+
 // Vector reduction into global memory (16-byte aligned address), sm_90+.
 __device__ __forceinline__ void red_add_v4(float* addr, float4 v) {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z),

@@ -89,9 +89,7 @@ __global__ void __launch_bounds__(kThreads) k_gradient(const float* __restrict__
         const float rr = cx + 2 < N ? __ldg(phi + idx + 2) : c;
         const float tt = cy >= 2 ? __ldg(phi + idx - 2 * N) : c;
         const float bb = cy + 2 < N ? __ldg(phi + idx + 2 * N) : c;
-        const float fx = (-rr + 8.0f * r - 8.0f * l + ll) / 12.0f;
-        const float fy = (-bb + 8.0f * b - 8.0f * t + tt) / 12.0f;
-        force[idx] = make_float2(fx * gmult, fy * gmult);
+        force[idx] = make_float2(diff4(ll, l, r, rr, gmult), diff4(tt, t, b, bb, gmult));
     }
 }
 
