@@ -12,8 +12,8 @@ seeded synthetic data of that shape.
 Prints ONE JSON line.  `value` is device-timed throughput (particle-steps/s)
 with the state resident in HBM; `e2e` is the same metric through the C ABI
 with host buffers: the state uploaded from page-locked host memory inside the
-timed region and the positions read back to page-locked host memory after
-every step.  --impl reference times the reference algorithm on the host
+timed region and the positions read back to page-locked host memory every
+--render-interval steps (2, the render cadence of the reference demo).  --impl reference times the reference algorithm on the host
 cores (the CPU restatement of CosmosCuda.cuh's step; the reference itself has
 no CPU step).  With N > 1 (torchrun) every rank runs an independent replica
 (the step is not sharded across GPUs).
@@ -182,6 +182,39 @@ def cpu_baseline(state, N, cic, dt, budget_s: float, min_steps: int = 2):
                       f"(FP32 restatement of the reference step, OpenMP over {threads} threads)"}
 
 
+def _cic_sample(F, x, y, N):
+    """Bilinear (CIC) sample of a force field at active particle positions, in
+    the reference's gather weights (CosmosCuda.cuh:263-278)."""
+    cx = np.trunc(x).astype(np.int64)
+    cy = np.trunc(y).astype(np.int64)
+    act = (cx >= 1) & (cx < N - 1) & (cy >= 1) & (cy < N - 1)
+    cx, cy = cx[act], cy[act]
+    fx = x[act].astype(np.float64) - cx
+    fy = y[act].astype(np.float64) - cy
+    Ff = F.reshape(N * N, 2).astype(np.float64)
+    c = cx + cy * N
+    return (Ff[c] * ((1 - fx) * (1 - fy))[:, None] + Ff[c + 1] * (fx * (1 - fy))[:, None]
+            + Ff[c + N] * ((1 - fx) * fy)[:, None] + Ff[c + N + 1] * (fx * fy)[:, None])
+
+
+def force_error_vs_fp64(state, N, cic, dt, F_gpu):
+    """Relative L2 error of the GPU force against the FP64 oracle on the same
+    positions: over the lattice, and sampled at the particles."""
+    from oracle import pm_oracle
+    pm_oracle.set_threads(os.cpu_count() or 1)
+    o = pm_oracle.OraclePM(N, cic, dt, 1.0, fp64=True)
+    o.deposit(state.x, state.y, state.m)
+    o.potential()
+    o.gradient()
+    ref = o.force()
+    o.close()
+    lattice = float(np.linalg.norm(F_gpu - ref) / np.linalg.norm(ref))
+    a = _cic_sample(F_gpu, state.x, state.y, N)
+    b = _cic_sample(ref, state.x, state.y, N)
+    particles = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return {"particles": particles, "lattice": lattice, "reference": "FP64 oracle (CPU) on the same positions"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -199,6 +232,13 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-interval", type=int, default=-1)
+    ap.add_argument("--force-mode", choices=["spectral", "gradient"], default="spectral",
+                    help="spectral: force from the FFT (<=1e-5 vs FP64); gradient: the reference's FP32 stencil")
+    ap.add_argument("--no-force-check", action="store_true", help="skip the FP64 force-accuracy check")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's kernels")
+    ap.add_argument("--ref-steps", type=int, default=20)
+    ap.add_argument("--render-interval", type=int, default=2,
+                    help="e2e: read the positions back every this many steps")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -234,9 +274,21 @@ def main():
     _build.build()
     rt = CudaRT()
     rt.lib.cudaSetDevice(local)
-    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=args.sort_interval)
+    mode = _lib.FORCE_SPECTRAL if args.force_mode == "spectral" else _lib.FORCE_GRADIENT
+    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=args.sort_interval, force_mode=mode)
     stream = sim.stream()
     sim.set_state(state)
+    config["force_mode"] = args.force_mode
+
+    # ---- force accuracy of this path against FP64 on the benchmark state ----
+    force_err = None
+    if rank == 0 and not args.no_force_check:
+        sim.run_stage(_lib.STAGE_DEPOSIT)
+        if mode == _lib.FORCE_GRADIENT:
+            sim.run_stage(_lib.STAGE_POTENTIAL)
+        sim.run_stage(_lib.STAGE_FORCE)
+        force_err = force_error_vs_fp64(state, N, cic, dt, sim.get_field(_lib.FIELD_FORCE))
+        sim.set_state(state)  # the stage hooks leave the state untouched; restart cleanly
 
     # ---- device-timed throughput (state resident) ----
     clk = ClockSampler(local).__enter__()
@@ -285,8 +337,9 @@ def main():
         # read x, y, xOld, yOld, m (20 B), write x, y, xOld, yOld (16 B); density clear 4 B/cell,
         # force window 8 B/cell, density flush 4 B/cell
         "fused_step": 36.0 * P + 16.0 * N * N,
-        # r2c rows 4+4, columns 4+2+4 (real K on a quarter: 1 B/cell), c2r rows 4+4
-        "fft_conv": 25.0 * N * N,
+        # gradient mode: r2c rows 4+4, columns 4+1+4 (real K on a quarter: 1 B/cell), c2r rows 4+4;
+        # spectral mode (force straight from the FFT): r2c 4+4, columns 4+1+8, c2r 8+8
+        "fft_conv": (37.0 if args.force_mode == "spectral" else 25.0) * N * N,
         "force": 12.0 * N * N,
     }
     dom = max(algo, key=lambda k: stages.get(k, 0.0))
@@ -307,36 +360,57 @@ def main():
             rt.pin(a)
         sim.synchronize()
         e2e_steps = args.steps
+        R = max(1, args.render_interval)
         t0 = time.perf_counter()
         sim.set_state(host_state)
         tickets = []
-        for _ in range(e2e_steps):
+        for i in range(e2e_steps):
             sim.step(1)
-            tickets.append(sim.positions_async(hx, hy, ordered=False))
+            if (i + 1) % R == 0 or i == e2e_steps - 1:
+                tickets.append(sim.positions_async(hx, hy, ordered=False))
         sim.wait(tickets[-1])
         sim.synchronize()
         t1 = time.perf_counter()
         for a in pinned:
             rt.unpin(a)
         e2e = {"value": P * e2e_steps / (t1 - t0), "unit": UNIT,
-               "h2d_bytes_per_step": int(20 * P / e2e_steps), "d2h_bytes_per_step": int(8 * P),
-               "note": "state uploaded once from page-locked memory (bytes amortised over the steps); "
-                       "x, y read back after every step"}
+               "h2d_bytes_per_step": int(20 * P / e2e_steps), "d2h_bytes_per_step": int(8 * P * len(tickets) / e2e_steps),
+               "note": f"state uploaded once from page-locked memory (bytes amortised over the steps); x, y read "
+                       f"back to page-locked memory every {R} steps (the reference demo renders every 2 steps)"}
     except Exception as exc:  # report, never hide
         e2e = {"value": None, "unit": UNIT, "error": str(exc)}
 
     launches = sim.launches_per_step() * args.steps
+    sim.close()
+
+    # ---- the reference's own step on the same GPU (its kernels + cuFFT) ----
+    ref_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        try:
+            from oracle import ref_oracle
+            if ref_oracle.available(N, dt):
+                with ref_oracle.RefGPU(N, cic, dt, P) as ref:
+                    ref.set_state(state)
+                    ref.time_steps(3)
+                    rms = ref.time_steps(args.ref_steps)
+                ref_gpu = {"ms_per_step": rms, "value": P / (rms / 1e3), "unit": UNIT, "steps": args.ref_steps,
+                           "source": "reference kernels (CosmosCuda.cuh) compiled for sm_103a + cuFFT, "
+                                     "Universe<K> step sequence, same GPU and state"}
+            else:
+                ref_gpu = {"unavailable": "reference PTX not built for this lattice/time step"}
+        except Exception as exc:
+            ref_gpu = {"unavailable": str(exc)}
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(state, N, cic, dt, args.cpu_budget)
-    sim.close()
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
-            "gpu_launches": launches, "stages_ms": stages}
+            "gpu_launches": launches, "stages_ms": stages, "reference_gpu": ref_gpu,
+            "force_rel_err_vs_fp64": force_err}
     print(json.dumps(line), flush=True)
 
 

@@ -52,6 +52,9 @@ struct cosmos_pm {
     float2* spec = nullptr;
     float* phi = nullptr;
     float2* force = nullptr;
+    float2* spec2 = nullptr;  // spectral mode: y-inverse of the Fy spectrum
+    float2* edge = nullptr;   // spectral mode: y-edge differences per line kx
+    float* dy = nullptr;      // spectral mode: y-edge differences per column x
     float* kq = nullptr;
     float2* tw = nullptr;
     double* diag = nullptr;
@@ -125,6 +128,24 @@ ParticleArrays& state(cosmos_pm* h) { return h->buf[h->cur]; }
 
 int sort_now(cosmos_pm* h);
 
+// Density -> force field.  Gradient mode: FFT convolution to the potential,
+// then the reference's edge-clamped stencil.  Spectral mode: the stencil is
+// applied in Fourier space (no potential field is written).  The profiling
+// event between the two halves marks the start of the force pass.
+int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
+    const float g = h->cfg.gravity_multiplier;
+    if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
+        CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
+                                            g, st));
+        if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
+    } else {
+        CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
+        if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
+        CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, g, st));
+    }
+    return COSMOS_OK;
+}
+
 // One step's kernels on stream st (buffer parity `cur`), assuming rho holds the
 // density of the current positions:
 //   FFT convolution rho -> phi, gradient phi -> force, clear rho,
@@ -137,9 +158,7 @@ int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
         return COSMOS_OK;
     };
     CPM_TRY(rec(kEvFft));
-    CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
-    CPM_TRY(rec(kEvForce));
-    CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
+    CPM_TRY(enqueue_force(h, st, profile));
     CPM_TRY(rec(kEvFused));
     CPM_CUDA(cudaMemsetAsync(h->rho, 0, NN * sizeof(float), st));
     if (h->items_valid)
@@ -284,6 +303,9 @@ void destroy_all(cosmos_pm* h) {
     cudaFree(h->spec);
     cudaFree(h->phi);
     cudaFree(h->force);
+    cudaFree(h->spec2);
+    cudaFree(h->edge);
+    cudaFree(h->dy);
     cudaFree(h->kq);
     cudaFree(h->tw);
     cudaFree(h->diag);
@@ -322,8 +344,8 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return cpm::fail(COSMOS_ERR_INVALID, "num_particles must be in [0, 2^32 - 16]");
     if (!std::isfinite(cfg->dt) || !std::isfinite(cfg->gravity_multiplier))
         return cpm::fail(COSMOS_ERR_INVALID, "dt and gravity_multiplier must be finite");
-    if (cfg->force_mode != COSMOS_FORCE_GRADIENT)
-        return cpm::fail(COSMOS_ERR_INVALID, "force_mode: only COSMOS_FORCE_GRADIENT is available");
+    if (cfg->force_mode != COSMOS_FORCE_GRADIENT && cfg->force_mode != COSMOS_FORCE_SPECTRAL)
+        return cpm::fail(COSMOS_ERR_INVALID, "force_mode must be COSMOS_FORCE_GRADIENT or COSMOS_FORCE_SPECTRAL");
     if (cfg->sort_granularity != -1 &&
         (cfg->sort_granularity < 4 || cfg->sort_granularity > 6 || (N >> cfg->sort_granularity) < 1))
         return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity must be -1 (default) or 4..6 with 2^g <= N");
@@ -411,6 +433,13 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         cudaMemsetAsync(h->force, 0, NN * sizeof(float2), h->stream) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "initialisation"));
     if (cpm::prepare_conv_passes(N) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "kernel attributes"));
+    if (cfg->force_mode == COSMOS_FORCE_SPECTRAL) {
+        if ((rc = dalloc(&h->spec2, NN / 2)) || (rc = dalloc(&h->edge, size_t(N / 2) * 4)) ||
+            (rc = dalloc(&h->dy, size_t(3) * N)))
+            return bail(rc);
+        if (cpm::prepare_spectral_passes(N) != cudaSuccess)
+            return bail(cpm::fail(COSMOS_ERR_CUDA, "spectral kernel attributes"));
+    }
     if ((rc = cpm::build_filter(N, h->cic, h->kq, h->tw, h->stream)) != COSMOS_OK) return bail(rc);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "create sync"));
     *out = h;
@@ -663,7 +692,12 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
                 CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
                 break;
             case COSMOS_STAGE_FORCE:
-                CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
+                // gradient mode: from the potential field; spectral mode: from the density
+                if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL)
+                    CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq,
+                                                        h->force, h->tw, h->cfg.gravity_multiplier, st));
+                else
+                    CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
                 break;
             case COSMOS_STAGE_INTEGRATE:
                 CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
@@ -813,8 +847,10 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream) {
 
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
     if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
-    // FFT passes + gradient + fused step kernel (the density clear is a memset node)
-    *launches = cpm::conv_launches_per_step() + 1 + 1;
+    // force passes + fused step kernel (the density clear is a memset node)
+    const int force = h->cfg.force_mode == COSMOS_FORCE_SPECTRAL ? cpm::spectral_launches_per_step()
+                                                                 : cpm::conv_launches_per_step() + 1;
+    *launches = force + 1;
     return COSMOS_OK;
 }
 

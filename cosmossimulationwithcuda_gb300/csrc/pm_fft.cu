@@ -168,30 +168,21 @@ __global__ void __launch_bounds__(NT, 1) k_cols_fwd_real64(const double2* __rest
 }
 
 // ---- pass 3: rows, half spectrum (transposed) -> real potential rows -----------------------
-template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
-                                                 const float2* __restrict__ tw) {
+// Hermitian pre-split of `lines` half spectra in shared memory (line stride
+// LinePad<M>): Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k]) is
+// twice the spectrum of z[n] = x[2n] + i x[2n+1]; pairs (k, M-k) in one thread.
+// Line element 0 holds the packed (X[0], X[N/2]).
+template <int M, int NT>
+__device__ __forceinline__ void c2r_presplit(float2* s, int lines, const float2* __restrict__ tw) {
     using C = float2;
-    constexpr int M = N / 2;
     constexpr int LP = LinePad<M>::value;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s = reinterpret_cast<C*>(smem_raw);
-    const int y0 = int(blockIdx.x) * B;
-    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
-        const int k = idx / B;
-        const int b = idx - k * B;
-        s[b * LP + pad16(k)] = spec[size_t(k) * N + y0 + b];
-    }
-    __syncthreads();
-    // Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k])  (twice the
-    // spectrum of z[n] = x[2n] + i x[2n+1]); pairs (k, M-k) in one thread.
     constexpr int H = M / 2 + 1;
-    for (int idx = threadIdx.x; idx < H * B; idx += NT) {
+    for (int idx = threadIdx.x; idx < H * lines; idx += NT) {
         const int b = idx / H;
         const int k = idx - b * H;
         C* row = s + b * LP;
         if (k == 0) {
-            const C x = row[0];  // (X[0], X[N/2])
+            const C x = row[0];
             row[0] = cmake<C>(x.x + x.y, x.x - x.y);
         } else {
             const C xk = row[pad16(k)];
@@ -208,11 +199,249 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const floa
             }
         }
     }
+}
+
+// B rows per CTA; the half spectrum is transposed: element (k, row) at
+// spec[k * STRIDE + row].
+template <int N, int B, int NT, int STRIDE = N>
+__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
+                                                 const float2* __restrict__ tw) {
+    using C = float2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<M>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int y0 = int(blockIdx.x) * B;
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int k = idx / B;
+        const int b = idx - k * B;
+        s[b * LP + pad16(k)] = spec[size_t(k) * STRIDE + y0 + b];
+    }
+    __syncthreads();
+    c2r_presplit<M, NT>(s, B, tw);
     __syncthreads();
     float2* orow = reinterpret_cast<float2*>(out + size_t(y0) * N);
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto gstore = [orow](int line, int i, C v) { orow[size_t(line) * M + i] = v; };
     fft_lines<M, B, NT, +1, C>(s, sload, gstore, tw, 2);
+}
+
+// ---- spectral force ---------------------------------------------------------------------------
+// The reference's 4th-order difference (CosmosCuda.cuh:174-229) is the
+// convolution with a stencil whose symbol is i*S(k), S = (8 sin t - sin 2t)/6,
+// t = 2 pi k / N.  Applying it in Fourier space gives the periodic force
+// straight out of the inverse FFT.  The reference clamps out-of-range
+// neighbours to the centre value instead of wrapping, which differs from the
+// periodic stencil only at x (or y) in {0, 1, N-2, N-1}; there the difference
+// is a combination of three potential differences along the line,
+//   D01 = phi(0) - phi(N-1),  D02 = phi(0) - phi(N-2),  D13 = phi(1) - phi(N-1),
+//   dF(0) = (-8 D01 + D02)/12,  dF(1) = D13/12,  dF(N-2) = D02/12,
+//   dF(N-1) = (D13 - 8 D01)/12   (times the gravity multiplier),
+// evaluated here as spectral sums so that no FP32 potential is differenced.
+//
+// Edge-difference weights at frequency k (table tw[k] = exp(-2 pi i k/N)):
+//   w01 = 1 - tw[k],  w02 = 1 - tw[2k],  w13 = conj(tw[k]) - tw[k].
+__device__ __forceinline__ void edge_weights(const float2* __restrict__ tw, int k, int N, float2& w01, float2& w02,
+                                             float2& w13) {
+    const float2 t1 = tw[k & (N - 1)];
+    const float2 t2 = tw[(2 * k) & (N - 1)];
+    w01 = make_float2(1.0f - t1.x, -t1.y);
+    w02 = make_float2(1.0f - t2.x, -t2.y);
+    w13 = make_float2(0.0f, -2.0f * t1.y);
+}
+
+// Sum of `v` over the CTA (NT threads); result valid in every thread.
+template <int NT, int K>
+__device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
+    constexpr int NW = NT / 32;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        for (int off = 16; off > 0; off >>= 1) v[j] += __shfl_xor_sync(0xffffffffu, v[j], off);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int j = 0; j < K; ++j) red[(threadIdx.x >> 5) * K + j] = v[j];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        float s = 0.0f;
+        for (int w = 0; w < NW; ++w) s += red[w * K + j];
+        v[j] = s;
+    }
+    __syncthreads();
+}
+
+// Columns, spectral force: forward FFT over y, x K, then two inverse FFTs over
+// y: Phi = IFFT_y(phi_hat) (back into spec) and Psi = IFFT_y(phi_hat * i S(ky) * g)
+// (into spec2); and the three y-edge differences of every line,
+// edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT, 1) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
+                                                         float2* __restrict__ edge, const float* __restrict__ kq,
+                                                         const float2* __restrict__ tw, float g) {
+    using C = float2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<N>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): phi_hat; [B, 2B): phi_hat * iS
+    float* red = reinterpret_cast<float*>(s + 2 * B * LP);
+    const int kx0 = int(blockIdx.x) * B;
+    C* lines = spec + size_t(kx0) * N;
+    auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
+    auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
+    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    for (int idx = threadIdx.x; idx < B * (M + 1); idx += NT) {
+        const int b = idx / (M + 1);
+        const int ky = idx - b * (M + 1);
+        const int kx = kx0 + b;
+        const int i1 = b * LP + pad16(ky);
+        const int i2 = b * LP + pad16((N - ky) & (N - 1));
+        if (kx != 0) {
+            const float kv = __ldg(kq + size_t(kx) * (M + 1) + ky);
+            s[i1] = cscale(s[i1], kv);
+            if (ky != 0 && ky != M) s[i2] = cscale(s[i2], kv);
+        } else {
+            const float k0 = __ldg(kq + ky);
+            const float km = __ldg(kq + size_t(M) * (M + 1) + ky);
+            const float p = 0.5f * (k0 + km), q = 0.5f * (k0 - km);
+            const C z1 = s[i1], z2 = s[i2];
+            s[i1] = cadd(cscale(z1, p), cscale(cconj(z2), q));
+            if (ky != 0 && ky != M) s[i2] = cadd(cscale(z2, p), cscale(cconj(z1), q));
+        }
+    }
+    __syncthreads();
+    for (int b = 0; b < B; ++b) {
+        float acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int ky = threadIdx.x; ky < N; ky += NT) {
+            const C v = s[b * LP + pad16(ky)];
+            C w01, w02, w13;
+            edge_weights(tw, ky, N, w01, w02, w13);
+            const C a = cmul(v, w01), c = cmul(v, w02), d = cmul(v, w13);
+            acc[0] += a.x; acc[1] += a.y; acc[2] += c.x; acc[3] += c.y; acc[4] += d.x; acc[5] += d.y;
+            // i * S(ky) * g, S = (8 sin t - sin 2t) / 6 with sin t = -tw[ky].y
+            const float S = g * (tw[(2 * ky) & (N - 1)].y - 8.0f * tw[ky].y) * (1.0f / 6.0f);
+            s[(B + b) * LP + pad16(ky)] = cmake<C>(-S * v.y, S * v.x);
+        }
+        block_sum<NT, 6>(acc, red);
+        if (threadIdx.x == 0) {
+            float2* e = edge + size_t(kx0 + b) * 4;
+            e[0] = make_float2(acc[0], acc[1]);
+            e[1] = make_float2(acc[2], acc[3]);
+            e[2] = make_float2(acc[4], acc[5]);
+        }
+    }
+    __syncthreads();
+    C* lines2 = spec2 + size_t(kx0) * N;
+    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
+    auto gstore2 = [lines, lines2](int line, int i, C v) {
+        if (line < B)
+            lines[size_t(line) * N + i] = v;
+        else
+            lines2[size_t(line - B) * N + i] = v;
+    };
+    fft_lines<N, 2 * B, NT, +1, C>(s, sload, gstore2, tw, 1);
+}
+
+// Rows, spectral force: C2R of Fx = IFFT_x(i S(kx) g Phi) and Fy = IFFT_x(Psi),
+// x-edge corrections from Phi, y-edge corrections from dy (the three y-edge
+// differences per column), written as interleaved (fx, fy).
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT, 1) k_rows_c2r_spectral(const float2* __restrict__ spec,
+                                                             const float2* __restrict__ spec2,
+                                                             const float* __restrict__ dy, float4* __restrict__ force,
+                                                             const float2* __restrict__ tw, float g) {
+    using C = float2;
+    constexpr int M = N / 2;
+    constexpr int LP = LinePad<M>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): Fx spectra, [B, 2B): Fy spectra
+    float* red = reinterpret_cast<float*>(s + 2 * B * LP);
+    __shared__ float dx[B][3];
+    const int y0 = int(blockIdx.x) * B;
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int k = idx / B;
+        const int b = idx - k * B;
+        s[b * LP + pad16(k)] = spec[size_t(k) * N + y0 + b];
+        s[(B + b) * LP + pad16(k)] = spec2[size_t(k) * N + y0 + b];
+    }
+    __syncthreads();
+    // x-edge differences of each row from its potential half spectrum:
+    // D = Phi(M) ((-1)^a - (-1)^b) + 2 sum_{k=1}^{M-1} Re(Phi(k) w(k))
+    for (int b = 0; b < B; ++b) {
+        float acc[3] = {0, 0, 0};
+        for (int k = 1 + threadIdx.x; k < M; k += NT) {
+            const C v = s[b * LP + pad16(k)];
+            C w01, w02, w13;
+            edge_weights(tw, k, N, w01, w02, w13);
+            acc[0] += v.x * w01.x - v.y * w01.y;
+            acc[1] += v.x * w02.x - v.y * w02.y;
+            acc[2] += v.x * w13.x - v.y * w13.y;
+        }
+        block_sum<NT, 3>(acc, red);
+        if (threadIdx.x == 0) {
+            const float pm = s[b * LP].y;  // Phi(N/2), real
+            dx[b][0] = 2.0f * acc[0] + 2.0f * pm;
+            dx[b][1] = 2.0f * acc[1];
+            dx[b][2] = 2.0f * acc[2];
+        }
+    }
+    __syncthreads();
+    // Fx spectrum = i S(kx) g Phi; S(0) = S(N/2) = 0 empties the packed element 0
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int b = idx / M;
+        const int k = idx - b * M;
+        C* p = s + b * LP + pad16(k);
+        if (k == 0) {
+            *p = cmake<C>(0.0f, 0.0f);
+        } else {
+            const float S = g * (tw[(2 * k) & (N - 1)].y - 8.0f * tw[k].y) * (1.0f / 6.0f);
+            const C v = *p;
+            *p = cmake<C>(-S * v.y, S * v.x);
+        }
+    }
+    __syncthreads();
+    c2r_presplit<M, NT>(s, 2 * B, tw);
+    __syncthreads();
+    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
+    auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
+    fft_lines<M, 2 * B, NT, +1, C>(s, sload, sstore, tw, 2);
+    // interleave, with the edge corrections
+    const float c12 = g * (1.0f / 12.0f);
+    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
+        const int b = idx / M;
+        const int i = idx - b * M;
+        const int y = y0 + b;
+        const C fx = s[b * LP + pad16(i)];        // (Fx[2i], Fx[2i+1])
+        const C fy = s[(B + b) * LP + pad16(i)];  // (Fy[2i], Fy[2i+1])
+        float4 o = make_float4(fx.x, fy.x, fx.y, fy.y);
+        if (i == 0) {  // x = 0, 1
+            o.x += (-8.0f * dx[b][0] + dx[b][1]) * c12;
+            o.z += dx[b][2] * c12;
+        } else if (i == M - 1) {  // x = N-2, N-1
+            o.x += dx[b][1] * c12;
+            o.z += (dx[b][2] - 8.0f * dx[b][0]) * c12;
+        }
+        if (y == 0 || y == 1 || y == N - 2 || y == N - 1) {
+            const int x0 = 2 * i;
+            const float d01a = dy[x0], d01b = dy[x0 + 1];
+            const float d02a = dy[N + x0], d02b = dy[N + x0 + 1];
+            const float d13a = dy[2 * N + x0], d13b = dy[2 * N + x0 + 1];
+            if (y == 0) {
+                o.y += (-8.0f * d01a + d02a) * c12;
+                o.w += (-8.0f * d01b + d02b) * c12;
+            } else if (y == 1) {
+                o.y += d13a * c12;
+                o.w += d13b * c12;
+            } else if (y == N - 2) {
+                o.y += d02a * c12;
+                o.w += d02b * c12;
+            } else {
+                o.y += (d13a - 8.0f * d01a) * c12;
+                o.w += (d13b - 8.0f * d01b) * c12;
+            }
+        }
+        force[(size_t(y) * N) / 2 + i] = o;
+    }
 }
 
 // ---- filter build helpers ----------------------------------------------------------------
@@ -273,6 +502,76 @@ static cudaError_t filter_passes_n(const double* g, double2* spec64, double* gha
 }
 
 #define CPM_FOR_EACH_N(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+
+// Spectral-force shapes: the passes keep two lines per transform in shared
+// memory (Fx and Fy, or phi_hat and phi_hat * iS), plus reduction scratch.
+template <int N>
+struct SpecShape {
+    using RS = RowShape<float, N>;
+    using CS = ColShape<float, N>;
+    static constexpr int M = N / 2;
+    static constexpr int RB0 = RS::B;
+    static constexpr size_t row_bytes0 = 2 * size_t(RB0) * LinePad<M>::value * sizeof(float2);
+    static constexpr int RB = row_bytes0 > 200 * 1024 ? RB0 / 2 : RB0;  // rows per CTA
+    static constexpr int RNT0 = RB * M / 8;
+    static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
+    static constexpr size_t row_smem = 2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + (RNT / 32) * 3 * 4;
+    static constexpr size_t col_smem = 2 * size_t(CS::B) * LinePad<N>::value * sizeof(float2) + (CS::NT / 32) * 6 * 4;
+    static constexpr int ENT0 = M / 8;
+    static constexpr int ENT = ENT0 < 64 ? 64 : (ENT0 > 1024 ? 1024 : ENT0);  // edge-row C2R threads
+    static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
+};
+
+template <int N>
+static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
+                                     const float* kq, float2* force, const float2* tw, float g, cudaStream_t st) {
+    using RS = RowShape<float, N>;
+    using CS = ColShape<float, N>;
+    using SS = SpecShape<N>;
+    k_rows_r2c<float, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_cols_spectral<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, SS::col_smem, st>>>(spec, spec2, edge, kq, tw, g);
+    k_rows_c2r<N, 1, SS::ENT, 4><<<3, SS::ENT, SS::edge_smem, st>>>(edge, dy, tw);
+    k_rows_c2r_spectral<N, SS::RB, SS::RNT><<<N / SS::RB, SS::RNT, SS::row_smem, st>>>(
+        spec, spec2, dy, reinterpret_cast<float4*>(force), tw, g);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t prepare_spectral_n() {
+    using CS = ColShape<float, N>;
+    using SS = SpecShape<N>;
+    cudaError_t e;
+    if ((e = allow_smem(k_cols_spectral<N, CS::B, CS::NT>, SS::col_smem)) != cudaSuccess) return e;
+    if ((e = allow_smem(k_rows_c2r<N, 1, SS::ENT, 4>, SS::edge_smem)) != cudaSuccess) return e;
+    return allow_smem(k_rows_c2r_spectral<N, SS::RB, SS::RNT>, SS::row_smem);
+}
+
+cudaError_t prepare_spectral_passes(int N) {
+    switch (N) {
+#define CPM_CASE(n) \
+    case n:         \
+        return prepare_spectral_n<n>();
+        CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
+                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st) {
+    switch (N) {
+#define CPM_CASE(n) \
+    case n:         \
+        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, st);
+        CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+int spectral_launches_per_step() { return 4; }
 
 template <int N>
 static cudaError_t prepare_conv_n() {

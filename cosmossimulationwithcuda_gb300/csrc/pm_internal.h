@@ -12,6 +12,13 @@ cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const floa
                                cudaStream_t st);
 int conv_launches_per_step();
 int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st);
+// Spectral force: density -> force field (interleaved fx, fy) with the
+// reference's clamped-edge stencil applied in Fourier space.  spec2: N*N/2
+// float2; edge: (N/2)*4 float2; dy: 3*N float.
+cudaError_t prepare_spectral_passes(int N);
+cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
+                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st);
+int spectral_launches_per_step();
 
 // pm_particles.cu
 struct ParticleArrays {
