@@ -33,14 +33,21 @@ struct LinePad {
 };
 
 template <int L>
-struct RadixPlan {
-    static constexpr int log2L = (L <= 1) ? 0 : 1 + RadixPlan<(L >> 1)>::log2L;
-    static constexpr int first = (log2L % 3 == 0) ? 8 : ((log2L % 3 == 1) ? 2 : 4);
+struct Log2 {
+    static constexpr int value = (L <= 1) ? 0 : 1 + Log2<(L >> 1)>::value;
 };
 template <>
-struct RadixPlan<1> {
-    static constexpr int log2L = 0;
-    static constexpr int first = 1;
+struct Log2<1> {
+    static constexpr int value = 0;
+};
+
+// Radix plan: one stage of radix 2^(log2 L mod log2 MAXR) (when nonzero),
+// then radix-MAXR stages (MAXR = 8 or 16).
+template <int L, int MAXR = 8>
+struct RadixPlan {
+    static constexpr int lr = MAXR == 16 ? 4 : 3;
+    static constexpr int rem = Log2<L>::value % lr;
+    static constexpr int first = rem == 0 ? MAXR : (1 << rem);
 };
 
 template <int DIR, class C>
@@ -86,6 +93,45 @@ __device__ __forceinline__ void dft8(C* v) {
     v[7] = csub(e3, o3);
 }
 
+// 16-point DFT as 4 x 4: DFT4 over n1 (stride 4), twiddle W16^(n1 k2), DFT4
+// over the other index; output in natural order.
+template <int DIR, class C>
+__device__ __forceinline__ void dft16(C* v) {
+    using R = decltype(C{}.x);
+    const R c1 = R(0.92387953251128675613), s1 = R(0.38268343236508977173), h = R(0.70710678118654752440);
+    C u[4][4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        u[n][0] = v[n];
+        u[n][1] = v[n + 4];
+        u[n][2] = v[n + 8];
+        u[n][3] = v[n + 12];
+        dft4<DIR>(u[n][0], u[n][1], u[n][2], u[n][3]);
+    }
+    // twiddles W16^(n k) for n, k in 1..3; W16 = exp(DIR * 2 pi i / 16)
+    const R sg = DIR < 0 ? R(-1) : R(1);
+    const C w1 = cmake<C>(c1, sg * s1), w2 = cmake<C>(h, sg * h), w3 = cmake<C>(s1, sg * c1);
+    const C w6 = cmake<C>(-h, sg * h), w9 = cmake<C>(-c1, -sg * s1);
+    u[1][1] = cmul(u[1][1], w1);
+    u[1][2] = cmul(u[1][2], w2);
+    u[1][3] = cmul(u[1][3], w3);
+    u[2][1] = cmul(u[2][1], w2);
+    u[2][2] = cmul_i<DIR>(u[2][2]);
+    u[2][3] = cmul(u[2][3], w6);
+    u[3][1] = cmul(u[3][1], w3);
+    u[3][2] = cmul(u[3][2], w6);
+    u[3][3] = cmul(u[3][3], w9);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        C a = u[0][k], b = u[1][k], c = u[2][k], d = u[3][k];
+        dft4<DIR>(a, b, c, d);
+        v[k] = a;
+        v[k + 4] = b;
+        v[k + 8] = c;
+        v[k + 12] = d;
+    }
+}
+
 template <int R, int DIR, class C>
 __device__ __forceinline__ void dft_r(C* v) {
     if constexpr (R == 2) {
@@ -94,6 +140,8 @@ __device__ __forceinline__ void dft_r(C* v) {
         dft4<DIR>(v[0], v[1], v[2], v[3]);
     } else if constexpr (R == 8) {
         dft8<DIR>(v);
+    } else if constexpr (R == 16) {
+        dft16<DIR>(v);
     }
 }
 
@@ -128,12 +176,24 @@ __device__ __forceinline__ void fft_stage(const Load& load, const Store& store, 
                     const C w3 = cmul(w2, w1);
                     v[q][2] = cmul(v[q][2], w2);
                     v[q][3] = cmul(v[q][3], w3);
-                    if constexpr (R == 8) {
+                    if constexpr (R >= 8) {
                         const C w4 = cmul(w2, w2);
                         v[q][4] = cmul(v[q][4], w4);
                         v[q][5] = cmul(v[q][5], cmul(w4, w1));
                         v[q][6] = cmul(v[q][6], cmul(w4, w2));
                         v[q][7] = cmul(v[q][7], cmul(w4, w3));
+                        if constexpr (R == 16) {
+                            const C w8 = cmul(w4, w4);
+                            const C w12 = cmul(w8, w4);
+                            v[q][8] = cmul(v[q][8], w8);
+                            v[q][9] = cmul(v[q][9], cmul(w8, w1));
+                            v[q][10] = cmul(v[q][10], cmul(w8, w2));
+                            v[q][11] = cmul(v[q][11], cmul(w8, w3));
+                            v[q][12] = cmul(v[q][12], w12);
+                            v[q][13] = cmul(v[q][13], cmul(w12, w1));
+                            v[q][14] = cmul(v[q][14], cmul(w12, w2));
+                            v[q][15] = cmul(v[q][15], cmul(w12, w3));
+                        }
                     }
                 }
             }
@@ -157,11 +217,11 @@ __device__ __forceinline__ void fft_stage(const Load& load, const Store& store, 
 }
 
 // Recursive driver: stage with sub-length Ns, then the rest.
-template <int L, int Ns, int B, int NT, int DIR, class C, class SrcLoad, class DstStore>
+template <int L, int Ns, int B, int NT, int DIR, class C, class SrcLoad, class DstStore, int MAXR>
 struct FftStages {
     static __device__ __forceinline__ void run(C* smem, const SrcLoad& src, const DstStore& dst,
                                                const C* __restrict__ tw, int tw_stride) {
-        constexpr int R = (Ns == 1) ? RadixPlan<L>::first : 8;
+        constexpr int R = (Ns == 1) ? RadixPlan<L, MAXR>::first : MAXR;
         constexpr int LP = LinePad<L>::value;
         auto sload = [smem](int line, int i) { return smem[line * LP + pad16(i)]; };
         auto sstore = [smem](int line, int i, C v) { smem[line * LP + pad16(i)] = v; };
@@ -176,16 +236,19 @@ struct FftStages {
         } else {
             fft_stage<L, R, Ns, B, NT, DIR, C>(sload, sstore, tw, tw_stride);
         }
-        if constexpr (!last) FftStages<L, Ns * R, B, NT, DIR, C, SrcLoad, DstStore>::run(smem, src, dst, tw, tw_stride);
+        if constexpr (!last)
+            FftStages<L, Ns * R, B, NT, DIR, C, SrcLoad, DstStore, MAXR>::run(smem, src, dst, tw, tw_stride);
     }
 };
 
 // Transform B lines: first stage reads through `src`, last stage writes through
-// `dst`, intermediate stages use `smem` (B * LinePad<L> elements).
-template <int L, int B, int NT, int DIR, class C, class SrcLoad, class DstStore>
+// `dst`, intermediate stages use `smem` (B * LinePad<L> elements).  MAXR is the
+// largest radix (8 or 16): radix-16 halves the shared-memory round trips of
+// radix-8 on long lines at the cost of more registers per thread.
+template <int L, int B, int NT, int DIR, class C, int MAXR = 8, class SrcLoad, class DstStore>
 __device__ __forceinline__ void fft_lines(C* smem, const SrcLoad& src, const DstStore& dst, const C* __restrict__ tw,
                                           int tw_stride) {
-    FftStages<L, 1, B, NT, DIR, C, SrcLoad, DstStore>::run(smem, src, dst, tw, tw_stride);
+    FftStages<L, 1, B, NT, DIR, C, SrcLoad, DstStore, MAXR>::run(smem, src, dst, tw, tw_stride);
 }
 
 }  // namespace cpm

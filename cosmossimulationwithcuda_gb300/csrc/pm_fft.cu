@@ -32,12 +32,15 @@
 namespace cpm {
 
 // ---- launch shapes ------------------------------------------------------------------
-// Launch shapes: about 4096 complex points per CTA (~35 KB of shared memory),
-// one radix-8 butterfly per thread per stage (so few registers per thread and
-// several CTAs per SM to hide the global-memory latency), and at least 4 rows
-// per CTA in the row passes so that the transposed spectrum moves in 32-byte
-// sectors.  FP64 (filter build) halves the rows to keep shared memory in range.
+// Launch shapes (chosen by timing variants at 2048^2): radix-16 Stockham
+// stages with one radix-16 butterfly per thread per stage, about 4096 points
+// per row CTA (at least 4 rows, so that the transposed spectrum moves in
+// 32-byte sectors) and one 2048-point line per column CTA, so that 4-6 CTAs
+// are resident per SM and their load / transform / store phases overlap.
+// FP64 (filter build) halves the rows to keep shared memory in range.
+constexpr int kMaxRadix = 16;
 constexpr int ceil_pow2_min(int v, int lo) { return v < lo ? lo : v; }
+constexpr int clamp_threads(int v) { return v < 64 ? 64 : (v > 1024 ? 1024 : v); }
 
 template <class T, int N>
 struct RowShape {
@@ -45,26 +48,28 @@ struct RowShape {
     static constexpr int Bf0 = ceil_pow2_min(4096 / M, 4);
     static constexpr int Bf = Bf0 > N ? N : Bf0;
     static constexpr int B = (sizeof(T) == 8 && Bf > 1) ? (Bf / 2) : Bf;  // rows per CTA
-    static constexpr int NT0 = B * M / 8;
-    static constexpr int NT = NT0 < 64 ? 64 : (NT0 > 1024 ? 1024 : NT0);
-    static constexpr int MINB = NT <= 512 ? 2 : 1;
+    static constexpr int NT = clamp_threads(B * M / kMaxRadix);
     static constexpr size_t smem = size_t(B) * LinePad<M>::value * sizeof(cplx_t<T>);
 };
 
 template <class T, int N>
 struct ColShape {
     static constexpr int M = N / 2;
-    static constexpr int B0 = ceil_pow2_min(4096 / N, 1);
+    static constexpr int B0 = ceil_pow2_min(2048 / N, 1);
     static constexpr int B = B0 > M ? M : B0;  // lines per CTA
-    static constexpr int NT0 = B * N / 8;
-    static constexpr int NT = NT0 < 64 ? 64 : (NT0 > 1024 ? 1024 : NT0);
-    static constexpr int MINB = NT <= 512 ? 2 : 1;
+    static constexpr int NT = clamp_threads(B * N / kMaxRadix);
     static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);
+};
+
+// Minimum resident CTAs per SM for a block size (register budget of launch bounds).
+template <int NT>
+struct MinBlocks {
+    static constexpr int value = NT <= 128 ? 6 : (NT <= 256 ? 4 : (NT <= 512 ? 2 : 1));
 };
 
 // ---- pass 1: rows, real -> half spectrum, transposed store --------------------------------
 template <class T, int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
+__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
                                                  const cplx_t<T>* __restrict__ tw) {
     using C = cplx_t<T>;
     constexpr int M = N / 2;
@@ -76,7 +81,7 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_r2c(const T* _
     const C* rows = reinterpret_cast<const C*>(in + size_t(y0) * N);
     auto src = [rows](int line, int i) { return rows[line * M + i]; };
     auto dst = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<M, B, NT, -1, C>(s, src, dst, tw, 2);
+    fft_lines<M, B, NT, -1, C, kMaxRadix>(s, src, dst, tw, 2);
     // X[k] = (Z[k] + conj Z[M-k])/2 - i/2 W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i/N)
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
@@ -98,7 +103,7 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_r2c(const T* _
 // ---- pass 2: columns, forward FFT x K x inverse FFT ----------------------------------------
 // kq: (N/2+1) x (N/2+1) floats, kq[kx*(M+1) + min(ky, N-ky)].
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
+__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
                                                   const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;
@@ -111,7 +116,7 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_cols_conv(float2* _
     auto gstore = [lines](int line, int i, C v) { lines[size_t(line) * N + i] = v; };
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    fft_lines<N, B, NT, -1, C, kMaxRadix>(s, gload, sstore, tw, 1);
     for (int idx = threadIdx.x; idx < B * (M + 1); idx += NT) {
         const int b = idx / (M + 1);
         const int ky = idx - b * (M + 1);
@@ -134,7 +139,7 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_cols_conv(float2* _
         }
     }
     __syncthreads();
-    fft_lines<N, B, NT, +1, C>(s, sload, gstore, tw, 1);
+    fft_lines<N, B, NT, +1, C, kMaxRadix>(s, sload, gstore, tw, 1);
 }
 
 // FP64 forward column FFT for the filter build: writes the real part of the
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(NT, 1) k_cols_fwd_real64(const double2* __rest
     const C* lines = spec + size_t(kx0) * N;
     auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    fft_lines<N, B, NT, -1, C, kMaxRadix>(s, gload, sstore, tw, 1);
     for (int idx = threadIdx.x; idx < B * N; idx += NT) {
         const int b = idx / N;
         const int ky = idx - b * N;
@@ -204,7 +209,7 @@ __device__ __forceinline__ void c2r_presplit(float2* s, int lines, const float2*
 // B rows per CTA; the half spectrum is transposed: element (k, row) at
 // spec[k * STRIDE + row].
 template <int N, int B, int NT, int STRIDE = N>
-__global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
+__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
                                                  const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(NT, (NT <= 512 ? 2 : 1)) k_rows_c2r(const floa
     float2* orow = reinterpret_cast<float2*>(out + size_t(y0) * N);
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto gstore = [orow](int line, int i, C v) { orow[size_t(line) * M + i] = v; };
-    fft_lines<M, B, NT, +1, C>(s, sload, gstore, tw, 2);
+    fft_lines<M, B, NT, +1, C, kMaxRadix>(s, sload, gstore, tw, 2);
 }
 
 // ---- spectral force ---------------------------------------------------------------------------
@@ -276,7 +281,7 @@ __device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
 // (into spec2); and the three y-edge differences of every line,
 // edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, 1) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
+__global__ void __launch_bounds__(NT, 3) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
                                                          float2* __restrict__ edge, const float* __restrict__ kq,
                                                          const float2* __restrict__ tw, float g) {
     using C = float2;
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(NT, 1) k_cols_spectral(float2* __restrict__ sp
     C* lines = spec + size_t(kx0) * N;
     auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<N, B, NT, -1, C>(s, gload, sstore, tw, 1);
+    fft_lines<N, B, NT, -1, C, kMaxRadix>(s, gload, sstore, tw, 1);
     for (int idx = threadIdx.x; idx < B * (M + 1); idx += NT) {
         const int b = idx / (M + 1);
         const int ky = idx - b * (M + 1);
@@ -339,14 +344,14 @@ __global__ void __launch_bounds__(NT, 1) k_cols_spectral(float2* __restrict__ sp
         else
             lines2[size_t(line - B) * N + i] = v;
     };
-    fft_lines<N, 2 * B, NT, +1, C>(s, sload, gstore2, tw, 1);
+    fft_lines<N, 2 * B, NT, +1, C, kMaxRadix>(s, sload, gstore2, tw, 1);
 }
 
 // Rows, spectral force: C2R of Fx = IFFT_x(i S(kx) g Phi) and Fy = IFFT_x(Psi),
 // x-edge corrections from Phi, y-edge corrections from dy (the three y-edge
 // differences per column), written as interleaved (fx, fy).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, 1) k_rows_c2r_spectral(const float2* __restrict__ spec,
+__global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
                                                              const float* __restrict__ dy, float4* __restrict__ force,
                                                              const float2* __restrict__ tw, float g) {
@@ -404,7 +409,7 @@ __global__ void __launch_bounds__(NT, 1) k_rows_c2r_spectral(const float2* __res
     __syncthreads();
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<M, 2 * B, NT, +1, C>(s, sload, sstore, tw, 2);
+    fft_lines<M, 2 * B, NT, +1, C, kMaxRadix>(s, sload, sstore, tw, 2);
     // interleave, with the edge corrections
     const float c12 = g * (1.0f / 12.0f);
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
@@ -513,11 +518,11 @@ struct SpecShape {
     static constexpr int RB0 = RS::B;
     static constexpr size_t row_bytes0 = 2 * size_t(RB0) * LinePad<M>::value * sizeof(float2);
     static constexpr int RB = row_bytes0 > 200 * 1024 ? RB0 / 2 : RB0;  // rows per CTA
-    static constexpr int RNT0 = RB * M / 8;
+    static constexpr int RNT0 = RB * M / kMaxRadix;
     static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
     static constexpr size_t row_smem = 2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + (RNT / 32) * 3 * 4;
     static constexpr size_t col_smem = 2 * size_t(CS::B) * LinePad<N>::value * sizeof(float2) + (CS::NT / 32) * 6 * 4;
-    static constexpr int ENT0 = M / 8;
+    static constexpr int ENT0 = M / kMaxRadix;
     static constexpr int ENT = ENT0 < 64 ? 64 : (ENT0 > 1024 ? 1024 : ENT0);  // edge-row C2R threads
     static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
 };
