@@ -41,6 +41,8 @@ struct cosmos_pm {
     int N = 0, logN = 0, cic = 0, nsm = 0, device = 0;
     int64_t P = 0, Pq = 0, Palloc = 0;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
+    cudaStream_t aux_stream = nullptr;                         // spectral mode: concurrent edge pass
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 
     ParticleArrays buf[2]{};
     int cur = 0;
@@ -136,7 +138,7 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
     if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
         CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
-                                            g, st));
+                                            g, st, h->aux_stream, h->fork_ev, h->join_ev));
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
@@ -290,6 +292,7 @@ void destroy_all(cosmos_pm* h) {
     DeviceGuard g(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
     for (auto& b : h->buf) {
         cudaFree(b.x);
         cudaFree(b.y);
@@ -328,6 +331,9 @@ void destroy_all(cosmos_pm* h) {
         if (e) cudaEventDestroy(e);
     for (auto& t : h->tickets) cudaEventDestroy(t.second);
     for (auto e : h->event_pool) cudaEventDestroy(e);
+    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+    if (h->join_ev) cudaEventDestroy(h->join_ev);
+    if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
 }
@@ -439,6 +445,10 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
             return bail(rc);
         if (cpm::prepare_spectral_passes(N) != cudaSuccess)
             return bail(cpm::fail(COSMOS_ERR_CUDA, "spectral kernel attributes"));
+        if (cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess)
+            return bail(cpm::fail(COSMOS_ERR_CUDA, "auxiliary stream"));
     }
     if ((rc = cpm::build_filter(N, h->cic, h->kq, h->tw, h->stream)) != COSMOS_OK) return bail(rc);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "create sync"));
@@ -695,7 +705,8 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
                 // gradient mode: from the potential field; spectral mode: from the density
                 if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL)
                     CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq,
-                                                        h->force, h->tw, h->cfg.gravity_multiplier, st));
+                                                        h->force, h->tw, h->cfg.gravity_multiplier, st,
+                                                        h->aux_stream, h->fork_ev, h->join_ev));
                 else
                     CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
                 break;

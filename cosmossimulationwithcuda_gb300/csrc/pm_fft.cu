@@ -347,13 +347,13 @@ __global__ void __launch_bounds__(NT, 3) k_cols_spectral(float2* __restrict__ sp
     fft_lines<N, 2 * B, NT, +1, C, kMaxRadix>(s, sload, gstore2, tw, 1);
 }
 
-// Rows, spectral force: C2R of Fx = IFFT_x(i S(kx) g Phi) and Fy = IFFT_x(Psi),
-// x-edge corrections from Phi, y-edge corrections from dy (the three y-edge
-// differences per column), written as interleaved (fx, fy).
+// Rows, spectral force: C2R of Fx = IFFT_x(i S(kx) g Phi) and Fy = IFFT_x(Psi)
+// with the x-edge corrections from Phi, written as interleaved (fx, fy).  The
+// y-edge corrections of rows 0, 1, N-2, N-1 follow in k_apply_edge_rows.
 template <int N, int B, int NT>
 __global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
-                                                             const float* __restrict__ dy, float4* __restrict__ force,
+                                                             float4* __restrict__ force,
                                                              const float2* __restrict__ tw, float g) {
     using C = float2;
     constexpr int M = N / 2;
@@ -370,52 +370,48 @@ __global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __res
         s[(B + b) * LP + pad16(k)] = spec2[size_t(k) * N + y0 + b];
     }
     __syncthreads();
-    // x-edge differences of each row from its potential half spectrum:
-    // D = Phi(M) ((-1)^a - (-1)^b) + 2 sum_{k=1}^{M-1} Re(Phi(k) w(k))
-    for (int b = 0; b < B; ++b) {
-        float acc[3] = {0, 0, 0};
-        for (int k = 1 + threadIdx.x; k < M; k += NT) {
-            const C v = s[b * LP + pad16(k)];
-            C w01, w02, w13;
-            edge_weights(tw, k, N, w01, w02, w13);
-            acc[0] += v.x * w01.x - v.y * w01.y;
-            acc[1] += v.x * w02.x - v.y * w02.y;
-            acc[2] += v.x * w13.x - v.y * w13.y;
-        }
-        block_sum<NT, 3>(acc, red);
-        if (threadIdx.x == 0) {
-            const float pm = s[b * LP].y;  // Phi(N/2), real
-            dx[b][0] = 2.0f * acc[0] + 2.0f * pm;
-            dx[b][1] = 2.0f * acc[1];
-            dx[b][2] = 2.0f * acc[2];
-        }
-    }
-    __syncthreads();
-    // Fx spectrum = i S(kx) g Phi; S(0) = S(N/2) = 0 empties the packed element 0
-    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
-        const int b = idx / M;
-        const int k = idx - b * M;
-        C* p = s + b * LP + pad16(k);
-        if (k == 0) {
-            *p = cmake<C>(0.0f, 0.0f);
-        } else {
-            const float S = g * (tw[(2 * k) & (N - 1)].y - 8.0f * tw[k].y) * (1.0f / 6.0f);
+    // One pass over the potential half spectra Phi: the x-edge differences
+    //   D = Phi(M) ((-1)^a - (-1)^b) + 2 sum_{k=1}^{M-1} Re(Phi(k) w(k))
+    // of every row, and the Fx spectrum i S(kx) g Phi in place (S(0) = S(N/2) = 0
+    // empties the packed element 0).
+    float acc[3 * B];
+#pragma unroll
+    for (int j = 0; j < 3 * B; ++j) acc[j] = 0.0f;
+    for (int k = threadIdx.x; k < M; k += NT) {
+        C w01, w02, w13;
+        edge_weights(tw, k, N, w01, w02, w13);
+        const float S = g * (tw[(2 * k) & (N - 1)].y - 8.0f * tw[k].y) * (1.0f / 6.0f);
+#pragma unroll
+        for (int b = 0; b < B; ++b) {
+            C* p = s + b * LP + pad16(k);
             const C v = *p;
-            *p = cmake<C>(-S * v.y, S * v.x);
+            if (k != 0) {
+                acc[3 * b + 0] += v.x * w01.x - v.y * w01.y;
+                acc[3 * b + 1] += v.x * w02.x - v.y * w02.y;
+                acc[3 * b + 2] += v.x * w13.x - v.y * w13.y;
+                *p = cmake<C>(-S * v.y, S * v.x);
+            } else {
+                acc[3 * b + 0] += v.y;  // Phi(N/2): (-1)^0 - (-1)^(N-1) = 2 with the factor 2 below
+                *p = cmake<C>(0.0f, 0.0f);
+            }
         }
     }
-    __syncthreads();
+    block_sum<NT, 3 * B>(acc, red);
+    if (threadIdx.x < B) {
+        dx[threadIdx.x][0] = 2.0f * acc[3 * threadIdx.x + 0];
+        dx[threadIdx.x][1] = 2.0f * acc[3 * threadIdx.x + 1];
+        dx[threadIdx.x][2] = 2.0f * acc[3 * threadIdx.x + 2];
+    }
     c2r_presplit<M, NT>(s, 2 * B, tw);
     __syncthreads();
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
     fft_lines<M, 2 * B, NT, +1, C, kMaxRadix>(s, sload, sstore, tw, 2);
-    // interleave, with the edge corrections
+    // interleave, with the x-edge corrections
     const float c12 = g * (1.0f / 12.0f);
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int b = idx / M;
         const int i = idx - b * M;
-        const int y = y0 + b;
         const C fx = s[b * LP + pad16(i)];        // (Fx[2i], Fx[2i+1])
         const C fy = s[(B + b) * LP + pad16(i)];  // (Fy[2i], Fy[2i+1])
         float4 o = make_float4(fx.x, fy.x, fx.y, fy.y);
@@ -426,27 +422,21 @@ __global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __res
             o.x += dx[b][1] * c12;
             o.z += (dx[b][2] - 8.0f * dx[b][0]) * c12;
         }
-        if (y == 0 || y == 1 || y == N - 2 || y == N - 1) {
-            const int x0 = 2 * i;
-            const float d01a = dy[x0], d01b = dy[x0 + 1];
-            const float d02a = dy[N + x0], d02b = dy[N + x0 + 1];
-            const float d13a = dy[2 * N + x0], d13b = dy[2 * N + x0 + 1];
-            if (y == 0) {
-                o.y += (-8.0f * d01a + d02a) * c12;
-                o.w += (-8.0f * d01b + d02b) * c12;
-            } else if (y == 1) {
-                o.y += d13a * c12;
-                o.w += d13b * c12;
-            } else if (y == N - 2) {
-                o.y += d02a * c12;
-                o.w += d02b * c12;
-            } else {
-                o.y += (d13a - 8.0f * d01a) * c12;
-                o.w += (d13b - 8.0f * d01b) * c12;
-            }
-        }
-        force[(size_t(y) * N) / 2 + i] = o;
+        force[(size_t(y0 + b) * N) / 2 + i] = o;
     }
+}
+
+// y-edge corrections of Fy on rows 0, 1, N-2, N-1 from the three y-edge
+// differences of every column (dy[j * N + x], j = D01, D02, D13).
+__global__ void k_apply_edge_rows(const float* __restrict__ dy, float2* __restrict__ force, int N, float g) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= N) return;
+    const float c12 = g * (1.0f / 12.0f);
+    const float d01 = dy[x], d02 = dy[N + x], d13 = dy[2 * N + x];
+    force[x].y += (-8.0f * d01 + d02) * c12;
+    force[size_t(N) + x].y += d13 * c12;
+    force[size_t(N - 2) * N + x].y += d02 * c12;
+    force[size_t(N - 1) * N + x].y += (d13 - 8.0f * d01) * c12;
 }
 
 // ---- filter build helpers ----------------------------------------------------------------
@@ -520,24 +510,36 @@ struct SpecShape {
     static constexpr int RB = row_bytes0 > 200 * 1024 ? RB0 / 2 : RB0;  // rows per CTA
     static constexpr int RNT0 = RB * M / kMaxRadix;
     static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
-    static constexpr size_t row_smem = 2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + (RNT / 32) * 3 * 4;
+    // two spectra per row, plus block_sum scratch: one slot per warp for each of the 3 * RB edge sums
+    static constexpr size_t row_smem =
+        2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + size_t(RNT / 32) * 3 * RB * sizeof(float);
     static constexpr size_t col_smem = 2 * size_t(CS::B) * LinePad<N>::value * sizeof(float2) + (CS::NT / 32) * 6 * 4;
     static constexpr int ENT0 = M / kMaxRadix;
     static constexpr int ENT = ENT0 < 64 ? 64 : (ENT0 > 1024 ? 1024 : ENT0);  // edge-row C2R threads
     static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
 };
 
+// The 3-row C2R of the y-edge differences only feeds the 4 boundary rows: it
+// runs on the auxiliary stream, concurrent with the main C2R pass (fork/join
+// with events, which CUDA-graph capture records as graph edges).
 template <int N>
 static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                     const float* kq, float2* force, const float2* tw, float g, cudaStream_t st) {
+                                     const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
+                                     cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
+    cudaError_t e;
     k_rows_r2c<float, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(rho, spec, tw);
     k_cols_spectral<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, SS::col_smem, st>>>(spec, spec2, edge, kq, tw, g);
-    k_rows_c2r<N, 1, SS::ENT, 4><<<3, SS::ENT, SS::edge_smem, st>>>(edge, dy, tw);
+    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
+    k_rows_c2r<N, 1, SS::ENT, 4><<<3, SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
+    if ((e = cudaEventRecord(join, aux)) != cudaSuccess) return e;
     k_rows_c2r_spectral<N, SS::RB, SS::RNT><<<N / SS::RB, SS::RNT, SS::row_smem, st>>>(
-        spec, spec2, dy, reinterpret_cast<float4*>(force), tw, g);
+        spec, spec2, reinterpret_cast<float4*>(force), tw, g);
+    if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
+    k_apply_edge_rows<<<(N + 255) / 256, 256, 0, st>>>(dy, force, N, g);
     return cudaGetLastError();
 }
 
@@ -564,11 +566,12 @@ cudaError_t prepare_spectral_passes(int N) {
 }
 
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st) {
+                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, st);
+        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, st, aux, fork, join);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:
@@ -576,7 +579,7 @@ cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2*
     }
 }
 
-int spectral_launches_per_step() { return 4; }
+int spectral_launches_per_step() { return 5; }
 
 template <int N>
 static cudaError_t prepare_conv_n() {

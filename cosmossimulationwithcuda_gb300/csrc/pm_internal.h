@@ -16,8 +16,10 @@ int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st)
 // reference's clamped-edge stencil applied in Fourier space.  spec2: N*N/2
 // float2; edge: (N/2)*4 float2; dy: 3*N float.
 cudaError_t prepare_spectral_passes(int N);
+// aux/fork/join: an auxiliary stream and two events for the concurrent edge pass.
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st);
+                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join);
 int spectral_launches_per_step();
 
 // pm_particles.cu
