@@ -153,6 +153,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def measured_traffic(kernel: str, P: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture
+    (profiles/traffic.json), scaled to P particles; None when not captured."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            rec = json.load(f)[kernel]
+        return float(rec["dram_bytes_per_particle"]) * P
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def measured_peak_gbs():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -347,7 +358,7 @@ def main():
     achieved = algo[dom] / (stages[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": algo[dom], "traffic": None}
+                "algorithmic_bytes_per_launch": algo[dom], "traffic": measured_traffic(dom, P)}
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
