@@ -29,7 +29,8 @@ EXPORTS = (
     "cosmos_pm_get_field", "cosmos_pm_set_field", "cosmos_pm_sort", "cosmos_pm_tile_keys",
     "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
-    "cosmos_tile_sort_noalloc",
+    "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
+    "cosmos_pm_host_alloc", "cosmos_pm_host_free",
 )
 NOALLOC_MAX_PARTICLES = 1 << 20
 
@@ -46,7 +47,8 @@ class Config(ctypes.Structure):
         ("sort_interval", ctypes.c_int32),
         ("sort_granularity", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("blur_r", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 6),
     ]
 
 
@@ -98,6 +100,10 @@ def load(path: str | None = None):
         "cosmos_pm_last_error": (ctypes.c_char_p, [_vp]),
         "cosmos_pm_version": (ctypes.c_char_p, []),
         "cosmos_tile_sort_noalloc": (ctypes.c_int, [_vp, _vp, i64, i32, i32, _vp, ctypes.c_uint64]),
+        "cosmos_pm_render_frame": (ctypes.c_int, [_vp, _f32p]),
+        "cosmos_pm_get_frame_async": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(ctypes.c_uint64)]),
+        "cosmos_pm_host_alloc": (ctypes.c_int, [i64, ctypes.POINTER(_vp)]),
+        "cosmos_pm_host_free": (ctypes.c_int, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -130,12 +136,12 @@ class Simulation:
 
     def __init__(self, N: int, P: int, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0,
                  device: int = 0, force_mode: int = FORCE_GRADIENT, sort_interval: int = -1,
-                 sort_granularity: int = -1, use_graph: bool = True):
+                 sort_granularity: int = -1, use_graph: bool = True, blur_r: int = 3):
         self.L = load()
         self.cfg = default_config(lattice_n=N, deposit=DEPOSIT_CIC if cic else DEPOSIT_NGP, dt=dt,
                                   gravity_multiplier=gravity_multiplier, num_particles=P, device=device,
                                   force_mode=force_mode, sort_interval=sort_interval,
-                                  sort_granularity=sort_granularity, use_graph=int(use_graph))
+                                  sort_granularity=sort_granularity, use_graph=int(use_graph), blur_r=blur_r)
         h = _vp()
         rc = self.L.cosmos_pm_create(ctypes.byref(self.cfg), ctypes.byref(h))
         if rc != COSMOS_OK:
@@ -204,6 +210,16 @@ class Simulation:
         self._check(self.L.cosmos_pm_wait(self.h, ticket))
 
     # -- stages and fields ----------------------------------------------------
+    def render_frame(self):
+        out = np.empty((self.N, self.N), np.float32)
+        self._check(self.L.cosmos_pm_render_frame(self.h, _ptr(out)))
+        return out
+
+    def frame_async(self, host_frame) -> int:
+        t = ctypes.c_uint64()
+        self._check(self.L.cosmos_pm_get_frame_async(self.h, _ptr(host_frame), ctypes.byref(t)))
+        return t.value
+
     def run_stage(self, stage: int):
         self._check(self.L.cosmos_pm_run_stage(self.h, stage))
 

@@ -90,6 +90,17 @@ struct cosmos_pm {
     bool have_times = false;
     bool prof_sorted = false, prof_prologue = false;
 
+    // display frames (allocated on the first render call)
+    int blur_r = 3;
+    float* rkern = nullptr;
+    float* blurred = nullptr;
+    float* frame[2] = {nullptr, nullptr};
+    uint32_t* rstate = nullptr;  // frame min / max keys + finished-CTA counter
+    float* rext = nullptr;       // running min / max across frames
+    cudaEvent_t frame_ready[2] = {nullptr, nullptr};
+    cudaEvent_t frame_done[2] = {nullptr, nullptr};
+    int frame_slot = 0;
+
     bool use_graph = true;
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer parity][tiled]
 
@@ -129,6 +140,7 @@ int dalloc(T** p, size_t n) {
 ParticleArrays& state(cosmos_pm* h) { return h->buf[h->cur]; }
 
 int sort_now(cosmos_pm* h);
+int issue_ticket(cosmos_pm* h, uint64_t* ticket);
 
 // Density -> force field.  Gradient mode: FFT convolution to the potential,
 // then the reference's edge-clamped stencil.  Spectral mode: the stencil is
@@ -323,6 +335,15 @@ void destroy_all(cosmos_pm* h) {
             if (h->graph[i][j]) cudaGraphExecDestroy(h->graph[i][j]);
     }
     cudaFree(h->rs.counts);
+    cudaFree(h->rkern);
+    cudaFree(h->blurred);
+    cudaFree(h->rstate);
+    cudaFree(h->rext);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(h->frame[i]);
+        if (h->frame_ready[i]) cudaEventDestroy(h->frame_ready[i]);
+        if (h->frame_done[i]) cudaEventDestroy(h->frame_done[i]);
+    }
     cudaFree(h->tstart);
     cudaFree(h->tend);
     cudaFree(h->items);
@@ -355,6 +376,8 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
     if (cfg->sort_granularity != -1 &&
         (cfg->sort_granularity < 4 || cfg->sort_granularity > 6 || (N >> cfg->sort_granularity) < 1))
         return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity must be -1 (default) or 4..6 with 2^g <= N");
+    if (cfg->blur_r != 0 && (cfg->blur_r < 1 || cfg->blur_r > 15 || cfg->blur_r % 2 == 0))
+        return cpm::fail(COSMOS_ERR_INVALID, "blur_r must be 0 (default 3) or odd in [1, 15]");
     int ndev = 0;
     CPM_CUDA(cudaGetDeviceCount(&ndev));
     if (cfg->device < 0 || cfg->device >= ndev) return cpm::fail(COSMOS_ERR_INVALID, "device ordinal out of range");
@@ -369,6 +392,7 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
     h->Pq = (h->P / 4) * 4;
     h->Palloc = ((h->P + 3) / 4) * 4;
     h->use_graph = cfg->use_graph != 0;
+    h->blur_r = cfg->blur_r != 0 ? cfg->blur_r : 3;
     h->gran = cfg->sort_granularity >= 0 ? cfg->sort_granularity : (N >= 64 ? 5 : 4);
     {
         const int T = N >> h->gran;
@@ -544,6 +568,11 @@ int positions_async_impl(cosmos_pm* h, float* hx, float* hy, int ordered, uint64
     CPM_CUDA(cudaMemcpyAsync(hx, h->stage[s][0], bytes, cudaMemcpyDeviceToHost, h->copy_stream));
     CPM_CUDA(cudaMemcpyAsync(hy, h->stage[s][1], bytes, cudaMemcpyDeviceToHost, h->copy_stream));
     CPM_CUDA(cudaEventRecord(h->stage_done[s], h->copy_stream));
+    return issue_ticket(h, ticket);
+}
+
+// A ticket for everything enqueued on the copy stream so far.
+int issue_ticket(cosmos_pm* h, uint64_t* ticket) {
     cudaEvent_t ev = nullptr;
     {
         std::lock_guard<std::mutex> lk(h->ticket_mu);
@@ -558,6 +587,71 @@ int positions_async_impl(cosmos_pm* h, float* hx, float* hy, int ordered, uint64
     *ticket = h->next_ticket++;
     h->tickets.emplace_back(*ticket, ev);
     return COSMOS_OK;
+}
+
+// Render buffers, blur weights and the running extremes, on first use.
+int ensure_render(cosmos_pm* h) {
+    if (h->rkern) return COSMOS_OK;
+    const size_t NN = size_t(h->N) * h->N;
+    const int R = h->blur_r;
+    int rc = COSMOS_OK;
+    if ((rc = dalloc(&h->blurred, NN)) || (rc = dalloc(&h->frame[0], NN)) || (rc = dalloc(&h->frame[1], NN)) ||
+        (rc = dalloc(&h->rstate, 3)) || (rc = dalloc(&h->rext, 2)))
+        return rc;
+    for (int i = 0; i < 2; ++i) {
+        CPM_CUDA(cudaEventCreateWithFlags(&h->frame_ready[i], cudaEventDisableTiming));
+        CPM_CUDA(cudaEventCreateWithFlags(&h->frame_done[i], cudaEventDisableTiming));
+    }
+    std::vector<float> w(size_t(R) * R);
+    cpm::render_weights(R, w.data());
+    float* k = nullptr;
+    if ((rc = dalloc(&k, w.size()))) return rc;
+    if (cudaMemcpy(k, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(k);
+        return cpm::fail(COSMOS_ERR_CUDA, "blur weights upload");
+    }
+    CPM_CUDA(cpm::render_init(h->rstate, h->rext, h->stream));
+    h->rkern = k;
+    return COSMOS_OK;
+}
+
+// Render the density of the current positions into device frame slot s.
+int enqueue_render(cosmos_pm* h, int s) {
+    CPM_TRY(ensure_render(h));
+    if (!h->density_valid) CPM_TRY(enqueue_prologue(h, h->stream));
+    CPM_CUDA(cpm::launch_render(h->rho, h->blurred, h->frame[s], h->rkern, h->blur_r, h->N, h->rstate, h->rext,
+                                h->stream));
+    return COSMOS_OK;
+}
+
+int render_frame_impl(cosmos_pm* h, float* host) {
+    if (!host) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    CPM_TRY(ensure_render(h));
+    const int s = h->frame_slot;
+    h->frame_slot ^= 1;
+    CPM_CUDA(cudaStreamWaitEvent(h->stream, h->frame_done[s], 0));
+    CPM_TRY(enqueue_render(h, s));
+    CPM_CUDA(cudaMemcpyAsync(host, h->frame[s], size_t(h->N) * h->N * sizeof(float), cudaMemcpyDeviceToHost,
+                             h->stream));
+    CPM_CUDA(cudaEventRecord(h->frame_done[s], h->stream));
+    CPM_CUDA(cudaStreamSynchronize(h->stream));
+    return COSMOS_OK;
+}
+
+int frame_async_impl(cosmos_pm* h, float* host, uint64_t* ticket) {
+    if (!host || !ticket) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    CPM_TRY(ensure_render(h));
+    const int s = h->frame_slot;
+    h->frame_slot ^= 1;
+    // the previous copy out of this slot must have left the device
+    CPM_CUDA(cudaStreamWaitEvent(h->stream, h->frame_done[s], 0));
+    CPM_TRY(enqueue_render(h, s));
+    CPM_CUDA(cudaEventRecord(h->frame_ready[s], h->stream));
+    CPM_CUDA(cudaStreamWaitEvent(h->copy_stream, h->frame_ready[s], 0));
+    CPM_CUDA(cudaMemcpyAsync(host, h->frame[s], size_t(h->N) * h->N * sizeof(float), cudaMemcpyDeviceToHost,
+                             h->copy_stream));
+    CPM_CUDA(cudaEventRecord(h->frame_done[s], h->copy_stream));
+    return issue_ticket(h, ticket);
 }
 
 // Returns the event of a ticket still outstanding, or nullptr if it completed.
@@ -607,6 +701,7 @@ void cosmos_pm_default_config(cosmos_pm_config* c) {
     c->sort_interval = -1;
     c->sort_granularity = -1;
     c->use_graph = 1;
+    c->blur_r = 3;
 }
 
 int cosmos_pm_create(const cosmos_pm_config* cfg, cosmos_pm** out) { return create_impl(cfg, out); }
@@ -671,6 +766,18 @@ int cosmos_pm_get_positions_async(cosmos_pm* h, float* hx, float* hy, int32_t or
     if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
     DeviceGuard g(h->device);
     return finish(h, positions_async_impl(h, hx, hy, ordered, ticket));
+}
+
+int cosmos_pm_render_frame(cosmos_pm* h, float* host_frame) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, render_frame_impl(h, host_frame));
+}
+
+int cosmos_pm_get_frame_async(cosmos_pm* h, float* host_frame, uint64_t* ticket) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, frame_async_impl(h, host_frame, ticket));
 }
 
 int cosmos_pm_poll(cosmos_pm* h, uint64_t ticket, int32_t* done) {
@@ -862,6 +969,23 @@ int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
     const int force = h->cfg.force_mode == COSMOS_FORCE_SPECTRAL ? cpm::spectral_launches_per_step()
                                                                  : cpm::conv_launches_per_step() + 1;
     *launches = force + 1;
+    return COSMOS_OK;
+}
+
+int cosmos_pm_host_alloc(int64_t bytes, void** out) {
+    if (!out) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (bytes <= 0) return cpm::fail(COSMOS_ERR_INVALID, "bytes must be positive");
+    if (cudaMallocHost(out, size_t(bytes)) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return cpm::fail(COSMOS_ERR_NOMEM, "page-locked allocation of " + std::to_string(bytes) + " bytes failed");
+    }
+    return COSMOS_OK;
+}
+
+int cosmos_pm_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) return cpm::fail(COSMOS_ERR_CUDA, "cudaFreeHost");
     return COSMOS_OK;
 }
 

@@ -98,4 +98,10 @@ cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, c
 cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
                                 float dt, int nsm, cudaStream_t st);
 
+// pm_render.cu -- display frame of the density (the reference's render chain)
+void render_weights(int R, float* w);
+cudaError_t render_init(uint32_t* state, float* extremes, cudaStream_t st);
+cudaError_t launch_render(const float* rho, float* blurred, float* frame, const float* kern, int R, int N,
+                          uint32_t* state, float* extremes, cudaStream_t st);
+
 }  // namespace cpm

@@ -72,7 +72,8 @@ typedef struct cosmos_pm_config {
                                    -1 = library default for this lattice/particle count */
     int32_t sort_granularity;   /* log2 of the tile edge (cells) used as sort key; -1 = default */
     int32_t use_graph;          /* 1 = replay each step from a captured CUDA graph */
-    int32_t reserved[7];
+    int32_t blur_r;             /* render blur width, odd, 1..15 (Constants::BLUR_R, :49); 0 = 3 */
+    int32_t reserved[6];
 } cosmos_pm_config;
 
 typedef struct cosmos_pm cosmos_pm; /* opaque handle (one Universe) */
@@ -126,6 +127,19 @@ int cosmos_pm_synchronize(cosmos_pm* h);
  * position readback (it renders a density frame, CosmosCuda.cuh:1343-1351). */
 int cosmos_pm_get_positions_async(cosmos_pm* h, float* host_x, float* host_y, int32_t ordered,
                                   uint64_t* ticket);
+
+/* Render a display frame of the current density (the density of the
+ * particles' current positions) into host_frame (N*N floats), with the
+ * reference's render chain: BLUR_R blur, frame min / max folded into running
+ * extremes, 1.8 * ((v - min) / (max - min))^0.25 (CosmosCuda.cuh:1249-1256,
+ * kernels :613-828).  Synchronous. */
+int cosmos_pm_render_frame(cosmos_pm* h, float* host_frame);
+
+/* The same frame, asynchronously: rendered on the step stream after the last
+ * enqueued step and copied to host_frame (page-locked for a truly
+ * asynchronous copy) on the copy stream.  Replaces the worker's frame push
+ * (CosmosCuda.cuh:1343-1351, pushFrame :1302-1308). */
+int cosmos_pm_get_frame_async(cosmos_pm* h, float* host_frame, uint64_t* ticket);
 
 /* *done = 1 when the copy behind `ticket` has landed in host memory. */
 int cosmos_pm_poll(cosmos_pm* h, uint64_t ticket, int32_t* done);
@@ -202,6 +216,11 @@ int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
 #define COSMOS_NOALLOC_MAX_PARTICLES (1 << 20)
 int cosmos_tile_sort_noalloc(const float* x_dev, const float* y_dev, int64_t n, int32_t lattice_n,
                              int32_t granularity, uint32_t* perm_dev, uint64_t stream);
+
+/* Page-locked host memory for the asynchronous readbacks (the reference's
+ * cudaMallocHost of frame_h, CosmosCuda.cuh:928-929).  *out = NULL on failure. */
+int cosmos_pm_host_alloc(int64_t bytes, void** out);
+int cosmos_pm_host_free(void* p);
 
 /* Message of the last error on this handle (or the last create failure when
  * h is NULL).  The string stays valid until the next call on the handle. */

@@ -138,3 +138,52 @@ def step(x, y, xo, yo, m, N: int, cic: bool, dt: float, gmult: float = 1.0):
     phi = potential(rho, cic)
     F = gradient(phi, gmult)
     return integrate(F, x, y, xo, yo, N, cic, dt), (rho, phi, F)
+
+
+def blur_weights(R: int) -> np.ndarray:
+    """Render blur kernel: 1/(r+1) for r < (R-1)/2, else 0 (CosmosCuda.cuh:954-966).
+
+    Returned as [iy][ix] (row = y offset), float32 like the reference's table."""
+    h = (R - 1) // 2
+    d = np.arange(-h, h + 1, dtype=np.float64)
+    r = np.sqrt(d[None, :] ** 2 + d[:, None] ** 2)
+    return np.where(r < h, 1.0 / (r + 1.0), 0.0).astype(np.float32)
+
+
+class Renderer:
+    """Display frame of a density lattice (CosmosCuda.cuh:1249-1256).
+
+    blur   k_calcBlurConvolution (:773-828): R x R weighted sum, zero outside
+    minmax k_resetMinMax / k_calcMinMax (:630-743): the maximum starts at
+           FLT_MIN and the block reduction pads its unused lanes with 0.0, so
+           the frame extremes are min(min, 0) and max(max, 0, FLT_MIN)
+    smooth k_initSmoothMinMax / k_smoothMinMax (:744-755): running extremes
+           across frames, starting at (1e35, -1)
+    scale  k_scaleWithMinMax (:756-772): 1.8 * ((v - lo) / (hi - lo))^0.25
+    The blur is summed in FP64 here; the frame is compared with a tolerance."""
+
+    def __init__(self, R: int = 3):
+        self.R = R
+        self.w = blur_weights(R).astype(np.float64)
+        self.lo, self.hi = np.float32(1e35), np.float32(-1.0)
+
+    def blur(self, rho: np.ndarray) -> np.ndarray:
+        N = rho.shape[0]
+        h = (self.R - 1) // 2
+        p = np.zeros((N + 2 * h, N + 2 * h))
+        p[h:h + N, h:h + N] = rho
+        out = np.zeros((N, N))
+        for iy in range(self.R):
+            for ix in range(self.R):
+                if self.w[iy, ix] != 0.0:
+                    out += self.w[iy, ix] * p[iy:iy + N, ix:ix + N]
+        return out
+
+    def __call__(self, rho: np.ndarray) -> np.ndarray:
+        b = self.blur(np.asarray(rho, np.float64))
+        fmin = min(float(b.min()), 0.0)
+        fmax = max(float(b.max()), 0.0, float(np.finfo(np.float32).tiny))
+        self.lo = np.float32(min(float(self.lo), fmin))
+        self.hi = np.float32(max(float(self.hi), fmax))
+        lo, hi = float(self.lo), float(self.hi)
+        return (1.8 * ((b - lo) / (hi - lo)) ** 0.25).astype(np.float32)

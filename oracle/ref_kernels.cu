@@ -42,3 +42,9 @@ template __global__ void Kernels::k_shiftLattice<REF_N>(ComplexVar*, float*, boo
 template __global__ void Kernels::k_calcGradientLattice<REF_N>(const float* const, float2* const);
 template __global__ void Kernels::k_forceMultiSampling<REF_N>(const float2* const, float* const, float* const,
                                                               float* const, float* const, const int, const bool);
+
+// The render chain (CosmosCuda.cuh:613-828, launched at :1250-1255).
+template __global__ void Kernels::k_calcBlurConvolution<3, REF_N>(const float* const __restrict__,
+                                                                 float* const __restrict__);
+template __global__ void Kernels::k_calcMinMax<REF_N>(float*);
+template __global__ void Kernels::k_scaleWithMinMax<REF_N>(float*, float*);

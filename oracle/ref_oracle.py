@@ -37,6 +37,7 @@ def lib():
         L.ref_get_state.argtypes = [ctypes.c_void_p] + [_f32p] * 4
         L.ref_get_fields.argtypes = [ctypes.c_void_p] + [_f32p] * 3
         L.ref_step.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ref_render.argtypes = [ctypes.c_void_p, _f32p, _f32p]
         L.ref_time_steps.restype = ctypes.c_float
         L.ref_time_steps.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib = L
@@ -89,6 +90,12 @@ class RefGPU:
         f = np.empty((N, N, 2), np.float32)
         self._check(lib().ref_get_fields(self.h, d, p, f))
         return d, p, f
+
+    def render(self, density):
+        """One display frame of `density` through the reference's render chain."""
+        frame = np.empty((self.N, self.N), np.float32)
+        self._check(lib().ref_render(self.h, np.ascontiguousarray(density, np.float32), frame))
+        return frame
 
     def time_steps(self, n: int) -> float:
         ms = lib().ref_time_steps(self.h, n)

@@ -15,14 +15,17 @@
 //                :1286-1287 k_multElementwiseLatticeFilter, k_divElementwiseLatticeFilter
 //                :1291      cufftExecC2C inverse
 //                :1297-1299 k_shiftLattice, k_calcGradientLattice, k_forceMultiSampling
-// The render chain (run once per NUM_TIME_STEPS_PER_RENDER steps, :1249-1256)
-// is not part of the step and is not run.  Kernels are looked up by their
-// demangled names in the loaded module.
+//   render       :1249-1256 k_getRealComponentOfLattice, k_calcBlurConvolution,
+//                           k_resetMinMax, k_calcMinMax, k_smoothMinMax,
+//                           k_scaleWithMinMax (ref_render, on a given density;
+//                           the running extremes start with k_initSmoothMinMax)
+// Kernels are looked up by their demangled names in the loaded module.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <cxxabi.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -66,7 +69,10 @@ const char* kKernels[] = {"k_generateFilterLattice",        "k_generateMassAssig
                           "k_scatterMassOnAccumulator",     "k_copyAccumulatorIntoLattice",
                           "k_getRealComponentOfLattice",    "k_multElementwiseLatticeFilter",
                           "k_divElementwiseLatticeFilter",  "k_shiftLattice",
-                          "k_calcGradientLattice",          "k_forceMultiSampling"};
+                          "k_calcGradientLattice",          "k_forceMultiSampling",
+                          "k_calcBlurConvolution",          "k_resetMinMax",
+                          "k_calcMinMax",                   "k_initSmoothMinMax",
+                          "k_smoothMinMax",                 "k_scaleWithMinMax"};
 
 struct Ref {
     int N = 0, P = 0;
@@ -78,15 +84,21 @@ struct Ref {
     int numBlocks = 0;
     float2 *lattice = nullptr, *filter = nullptr, *deconv = nullptr, *forceXY = nullptr;
     float *acc = nullptr, *shifted = nullptr, *localForce = nullptr;
+    float *render1 = nullptr, *render2 = nullptr;  // renderOutput_d, renderOutput2_d
     float *x = nullptr, *y = nullptr, *xo = nullptr, *yo = nullptr, *m = nullptr;
 };
 
-int launch(Ref* r, const char* name, std::vector<void*> args) {
+int launch_shape(Ref* r, const char* name, dim3 grid, dim3 block, unsigned smem, std::vector<void*> args) {
     auto it = r->fn.find(name);
     if (it == r->fn.end()) return fail(std::string("kernel not found: ") + name);
-    RR_CU(cuLaunchKernel(it->second, r->numBlocks, 1, 1, 768, 1, 1, 0, reinterpret_cast<CUstream>(r->st),
-                         args.data(), nullptr));
+    RR_CU(cuLaunchKernel(it->second, grid.x, grid.y, grid.z, block.x, block.y, block.z, smem,
+                         reinterpret_cast<CUstream>(r->st), args.data(), nullptr));
     return 0;
+}
+
+// The reference's usual shape: numBlocks x THREADS (768).
+int launch(Ref* r, const char* name, std::vector<void*> args) {
+    return launch_shape(r, name, dim3(r->numBlocks), dim3(768), 0, std::move(args));
 }
 
 int load_module(Ref* r, const char* ptx_path) {
@@ -107,9 +119,12 @@ int load_module(Ref* r, const char* ptx_path) {
         char* dem = abi::__cxa_demangle(mangled, nullptr, nullptr, &status);
         const std::string d = (status == 0 && dem) ? dem : mangled;
         std::free(dem);
-        for (const char* k : kKernels) {
-            const std::string key = std::string("Kernels::") + k + "<";
-            if (d.find(key) != std::string::npos) r->fn[k] = f1;
+        for (const char* k : kKernels) {  // templates end in '<', plain kernels in '('
+            const std::string key = std::string("Kernels::") + k;
+            const size_t at = d.find(key);
+            if (at != std::string::npos && at + key.size() < d.size() &&
+                (d[at + key.size()] == '<' || d[at + key.size()] == '('))
+                r->fn[k] = f1;
         }
     }
     for (const char* k : kKernels)
@@ -138,6 +153,26 @@ int create(Ref* r, const char* ptx_path, int N, int cic, int P) {
     RR_RT(cudaMalloc(&r->acc, NN * sizeof(float)));
     RR_RT(cudaMalloc(&r->shifted, NN * sizeof(float)));
     RR_RT(cudaMalloc(&r->localForce, NN * sizeof(float)));
+    RR_RT(cudaMalloc(&r->render1, NN * sizeof(float)));
+    RR_RT(cudaMalloc(&r->render2, NN * sizeof(float)));
+    // the reference's blur grid covers no tile when N < 1024; keep that frame defined
+    RR_RT(cudaMemsetAsync(r->render2, 0, NN * sizeof(float), r->st));
+    if (launch_shape(r, "k_initSmoothMinMax", dim3(1), dim3(1), 0, {})) return -1;
+    // blur weights into the module's __constant__ table, as the constructor
+    // does (:954-966, :981): 1/(r+1) for r < BLUR_HALF_R, BLUR_R = 3
+    {
+        CUdeviceptr kern = 0;
+        size_t bytes = 0;
+        RR_CU(cuModuleGetGlobal(&kern, &bytes, r->mod, "_ZN7Kernels16renderBlurKern_cE"));
+        float w[9];
+        for (int iy = -1; iy <= 1; ++iy)
+            for (int ix = -1; ix <= 1; ++ix) {
+                const double rr = std::sqrt(double(ix * ix + iy * iy));
+                w[(ix + 1) + (iy + 1) * 3] = rr < 1 ? float(1.0 / (rr + 1.0)) : 0.0f;
+            }
+        if (bytes != sizeof(w)) return fail("renderBlurKern_c has an unexpected size");
+        RR_CU(cuMemcpyHtoD(kern, w, sizeof(w)));
+    }
     for (float** p : {&r->x, &r->y, &r->xo, &r->yo, &r->m}) RR_RT(cudaMalloc(p, size_t(P > 0 ? P : 1) * sizeof(float)));
     RR_RT(cudaMemsetAsync(r->acc, 0, NN * sizeof(float), r->st));
     RR_RT(cudaMemsetAsync(r->lattice, 0, NN * sizeof(float2), r->st));
@@ -179,11 +214,25 @@ int step_once(Ref* r) {
     return 0;
 }
 
+// One frame of the render chain on a density lattice already in r->acc.
+int render_once(Ref* r) {
+    if (launch(r, "k_copyAccumulatorIntoLattice", {&r->acc, &r->lattice})) return -1;
+    if (launch(r, "k_getRealComponentOfLattice", {&r->lattice, &r->render1})) return -1;
+    const unsigned smem = sizeof(float) * (3 + 32) * (3 + 32);  // BLUR_R = 3, TILE_SIZE = 32
+    if (launch_shape(r, "k_calcBlurConvolution", dim3(32, 32), dim3(32, 32), smem, {&r->render1, &r->render2}))
+        return -1;
+    if (launch_shape(r, "k_resetMinMax", dim3(1), dim3(1), 0, {})) return -1;
+    if (launch(r, "k_calcMinMax", {&r->render2})) return -1;
+    if (launch_shape(r, "k_smoothMinMax", dim3(1), dim3(1), 0, {})) return -1;
+    if (launch(r, "k_scaleWithMinMax", {&r->render2, &r->render1})) return -1;
+    return 0;
+}
+
 void destroy(Ref* r) {
     if (r->st) cudaStreamSynchronize(r->st);
     if (r->plan) cufftDestroy(r->plan);
     for (void* p : {(void*)r->lattice, (void*)r->filter, (void*)r->deconv, (void*)r->forceXY, (void*)r->acc,
-                    (void*)r->shifted, (void*)r->localForce, (void*)r->x, (void*)r->y, (void*)r->xo, (void*)r->yo,
+                    (void*)r->shifted, (void*)r->localForce, (void*)r->render1, (void*)r->render2, (void*)r->x, (void*)r->y, (void*)r->xo, (void*)r->yo,
                     (void*)r->m})
         cudaFree(p);
     if (r->mod) cuModuleUnload(r->mod);
@@ -249,6 +298,18 @@ int ref_step(void* h, int nsteps) {
     Ref* r = static_cast<Ref*>(h);
     for (int i = 0; i < nsteps; ++i)
         if (step_once(r)) return -1;
+    RR_RT(cudaStreamSynchronize(r->st));
+    return 0;
+}
+
+// Render one display frame of `density` (N*N floats) into `frame` with the
+// reference's render chain; the running min / max persist across calls.
+int ref_render(void* h, const float* density, float* frame) {
+    Ref* r = static_cast<Ref*>(h);
+    const size_t NN = size_t(r->N) * r->N;
+    RR_RT(cudaMemcpyAsync(r->acc, density, NN * sizeof(float), cudaMemcpyHostToDevice, r->st));
+    if (render_once(r)) return -1;
+    RR_RT(cudaMemcpyAsync(frame, r->render1, NN * sizeof(float), cudaMemcpyDeviceToHost, r->st));
     RR_RT(cudaStreamSynchronize(r->st));
     return 0;
 }

@@ -8,6 +8,10 @@ inputs and outputs as tests/golden/<case>.npz:
   after step 1: density, potential, force (the lattices of the first step) and
               x1, y1, x_old1, y_old1
   after `steps`: xk, yk, x_oldk, y_oldk
+and the render chain's frames as tests/golden/render<N>.npz: a sequence of
+seeded density lattices (render_density) rendered one after another (the
+running min / max carry over), stored as the values at fixed sampled cells;
+the SHA-256 of every full frame goes into the manifest.
 Needs a GPU and the reference PTX (oracle/_ref, built by oracle/ref_build.py
 where the reference sources are present).
 
@@ -16,6 +20,7 @@ where the reference sources are present).
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import sys
@@ -67,6 +72,38 @@ def make_inputs(N, dt, P, kind, seed):
     return dict(x=x, y=y, x_old=f(x - vx * dt), y_old=f(y - vy * dt), m=f(m))
 
 
+# render cases: name: (N, [(seed, scale) per frame]); the reference's blur grid
+# covers the lattice only for N >= 1024
+RENDER_CASES = {
+    "render2048": (2048, [(21, 1e-4), (22, 3e-4), (23, 5e-5)]),
+}
+RENDER_DT = 0.001  # any reference PTX of this N will do; the render chain ignores dt
+RENDER_SAMPLES = 8192
+
+
+def _splitmix64(v: np.ndarray) -> np.ndarray:
+    """SplitMix64 finaliser (Steele, Lea, Flood 2014) on uint64 arrays."""
+    with np.errstate(over="ignore"):
+        z = v + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def render_density(N: int, seed: int, scale: float) -> np.ndarray:
+    """Platform-independent seeded density lattice: a quarter of the cells hold
+    a uniform value in [0, scale), the rest are empty."""
+    h = _splitmix64(np.arange(N * N, dtype=np.uint64) + np.uint64(seed) * np.uint64(1 << 40))
+    u = (h >> np.uint64(11)).astype(np.float64) * (1.0 / (1 << 53))
+    occupied = (h & np.uint64(3)) == 0
+    return np.where(occupied, u * scale, 0.0).astype(np.float32).reshape(N, N)
+
+
+def render_sample_cells(N: int) -> np.ndarray:
+    h = _splitmix64(np.arange(RENDER_SAMPLES, dtype=np.uint64) + np.uint64(7))
+    return (h % np.uint64(N * N)).astype(np.int64)
+
+
 class _S:
     def __init__(self, d):
         self.__dict__.update(d)
@@ -75,10 +112,17 @@ class _S:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
+    ap.add_argument("--render-only", action="store_true",
+                    help="remake only the render fixtures; keep the step cases of the manifest")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     manifest = {}
+    if args.render_only:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "manifest.json")) as f:
+            manifest = json.load(f)["cases"]
     for name, (N, cic, dt, P, steps, kind, seed) in CASES.items():
+        if args.render_only:
+            break
         inp = make_inputs(N, dt, P, kind, seed)
         with ref_oracle.RefGPU(N, cic, dt, P) as ref:
             ref.set_state(_S(inp))
@@ -93,9 +137,21 @@ def main():
         np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
         manifest[name] = dict(N=N, cic=cic, dt=dt, P=P, steps=steps, kind=kind, seed=seed, fields=N <= 128)
         print(name, "ok", flush=True)
+    render = {}
+    for name, (N, frames) in RENDER_CASES.items():
+        cells = render_sample_cells(N)
+        values, digests = [], []
+        with ref_oracle.RefGPU(N, False, RENDER_DT, 4) as ref:
+            for seed, scale in frames:
+                frame = ref.render(render_density(N, seed, scale))
+                values.append(frame.reshape(-1)[cells])
+                digests.append(hashlib.sha256(frame.tobytes()).hexdigest())
+        np.savez_compressed(os.path.join(args.out, f"{name}.npz"), cells=cells, values=np.stack(values))
+        render[name] = dict(N=N, blur_r=3, frames=[[seed, scale] for seed, scale in frames], sha256=digests)
+        print(name, "ok", flush=True)
     with open(os.path.join(args.out, "manifest.json"), "w") as f:
         json.dump({"source": "reference kernels (CosmosCuda.cuh) compiled for sm_103a + cuFFT, "
-                             "run by oracle/ref_runner.cpp", "cases": manifest}, f, indent=1)
+                             "run by oracle/ref_runner.cpp", "cases": manifest, "render": render}, f, indent=1)
 
 
 if __name__ == "__main__":

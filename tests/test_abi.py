@@ -44,3 +44,22 @@ def test_version_and_default_config(cosmos_lib):
     c = cosmos_lib.default_config()
     assert c.lattice_n == 2048 and c.deposit == cosmos_lib.DEPOSIT_CIC and c.use_graph == 1
     assert ctypes.sizeof(cosmos_lib.Config) == 4 * 4 + 8 + 4 * 5 + 4 * 7  # matches cosmos_pm_config
+
+
+def test_default_blur_width(cosmos_lib):
+    assert cosmos_lib.default_config().blur_r == 3
+
+
+def test_universe_dropin_header_compiles():
+    """include/CosmosGB300.cuh (the Universe<K> drop-in) compiles with plain
+    g++ as the reference's user code would include it."""
+    import shutil
+    import subprocess
+    import pytest
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "universe_test.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -96,3 +96,23 @@ def test_cuda_path_matches_reference_kernels(cosmos_lib, name):
             s.synchronize()
             sk = s.get_particles()[:4]
         check_against_golden(name, c, d, fields, s1, sk)
+
+
+def _render_cases():
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f).get("render", {})
+
+
+@pytest.mark.parametrize("name", sorted(_render_cases()))
+def test_render_oracle_vs_reference_frames(name):
+    """The numpy render chain (oracle/pm_np.py Renderer) against the frames the
+    reference's own render kernels made, at the sampled cells."""
+    from oracle import pm_np
+    from tests.golden.make_golden import render_density
+    c = _render_cases()[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    ren = pm_np.Renderer(c["blur_r"])
+    N = c["N"]
+    for k, (seed, scale) in enumerate(c["frames"]):
+        frame = ren(render_density(N, seed, scale))
+        assert np.abs(frame.reshape(-1)[g["cells"]] - g["values"][k]).max() <= 2e-5
