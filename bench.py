@@ -226,6 +226,96 @@ def force_error_vs_fp64(state, N, cic, dt, F_gpu):
     return {"particles": particles, "lattice": lattice, "reference": "FP64 oracle (CPU) on the same positions"}
 
 
+IC_TEXT = {
+    "disk-20M-2048-cic": "exponential disk, scale 200 cells, v_c from enclosed mass + 5% dispersion, "
+                         "lognormal(0,0.3) masses",
+    "uniform-1M-512-ngp": "uniform on the lattice, Gaussian velocities, lognormal(0,0.3) masses",
+    "collide-100M-4096-cic": "two counter-rotating exponential disks (scale 300), approaching",
+    "clumpy-1B-8192-cic": "uniform background + 32 Plummer clumps (a = 40 cells, 2% of the mass each), at rest",
+}
+
+
+def run_ensemble(args, ws, rank, local):
+    """The 64-simulation ensemble: device-timed steps of all simulations (one
+    graph launch per step), particle-steps/s summed over the simulations."""
+    from cosmossimulationwithcuda_gb300 import _build, _lib, ics
+    e = ics.ENSEMBLE
+    Ns, Ps, states = ics.ensemble_workload()
+    Ptot = int(sum(Ps))
+    _build.build()
+    rt = CudaRT()
+    rt.lib.cudaSetDevice(local)
+    mode = _lib.FORCE_SPECTRAL if args.force_mode == "spectral" else _lib.FORCE_GRADIENT
+    ens = _lib.Ensemble(Ns, Ps, cic=e["cic"], dt=e["dt"], device=local, force_mode=mode,
+                        sort_interval=args.sort_interval if args.sort_interval > 0 else 32)
+    for i, st in enumerate(states):
+        ens.set_state(i, st)
+    stream = ens.stream()
+    steps = args.steps
+    clk = ClockSampler(local).__enter__()
+    ens.step(args.warmup)
+    ens.synchronize()
+    clk.wait_first()
+    e0, e1 = rt.event(), rt.event()
+    try:
+        rt.record(e0, stream)
+        ens.step(steps)
+        rt.record(e1, stream)
+        ms = rt.elapsed_ms(e0, e1)
+    finally:
+        clk.__exit__()
+    ens.synchronize()
+    launches = ens.launches_per_step() * steps
+    # whole-step algorithmic bytes: fused step 36 B/particle + 16 B/cell; force passes 37 B/cell (spectral:
+    # FFT passes; gradient: 25 B/cell of FFT passes + 12 B/cell of stencil)
+    cells = float(sum(n * n for n in Ns))
+    algo = 36.0 * Ptot + (16.0 + 37.0) * cells
+    peak, peak_kind = measured_peak_gbs()
+    achieved = algo / (ms / steps / 1e3) / 1e9
+    # end to end: upload every simulation's state from page-locked memory, step, read positions back
+    host = [st.copy() for st in states]
+    pinned = [a for st in host for a in (st.x, st.y, st.x_old, st.y_old, st.m)]
+    for a in pinned:
+        rt.pin(a)
+    e2e_steps = min(steps, 50)
+    t0 = time.perf_counter()
+    for i, st in enumerate(host):
+        ens.set_state(i, st)
+    ens.step(e2e_steps)
+    outs = [ens.get_particles(i, count=None)[:2] for i in range(len(Ns))]
+    t1 = time.perf_counter()
+    for a in pinned:
+        rt.unpin(a)
+    ens.close()
+    del outs
+    cb = None
+    if not args.no_cpu_baseline:
+        # the reference algorithm on the host cores for the largest simulation (bounded sample)
+        j = int(np.argmax(Ps))
+        cb = cpu_baseline(states[j], Ns[j], e["cic"], e["dt"], args.cpu_budget)
+        cb["sample"] = "simulation %d of the ensemble (N=%d, P=%d): " % (j, Ns[j], Ps[j]) + cb["sample"]
+    if rank != 0:
+        return
+    value = Ptot * steps * ws / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": e["name"], "sims": len(Ns), "particles_total": Ptot,
+                       "lattices": {str(n): int(sum(1 for m in Ns if m == n)) for n in sorted(set(Ns))},
+                       "p_min": int(min(Ps)), "p_max": int(max(Ps)), "deposit": "CIC", "dt": e["dt"],
+                       "force_mode": args.force_mode, "ic": "alternating binary (2 Plummer, 1:0.6) / exponential disk",
+                       "l2": f"particle state {20 * Ptot / 1e6:.0f} MB exceeds the 126 MB L2"},
+            "roofline": {"bound": "hbm", "kernel": "whole ensemble step", "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": algo, "traffic": None},
+            "cpu_baseline": cb,
+            "e2e": {"value": Ptot * e2e_steps / (t1 - t0), "unit": UNIT,
+                    "h2d_bytes_per_step": int(20 * Ptot / e2e_steps), "d2h_bytes_per_step": int(20 * Ptot / e2e_steps),
+                    "note": f"all states uploaded from page-locked memory, {e2e_steps} steps, all particles read back"},
+            "clocks": clk.summary(), "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -250,6 +340,10 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--render-interval", type=int, default=2,
                     help="e2e: read the positions back every this many steps")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    help="the headline disk (default), another single-simulation workload "
+                         "(uniform-1M-512-ngp, collide-100M-4096-cic, clumpy-1B-8192-cic) or "
+                         "ensemble-64-mixed-cic")
     args = ap.parse_args()
 
     ws, rank, local = dist_env()
@@ -259,14 +353,18 @@ def main():
 
     from cosmossimulationwithcuda_gb300 import ics
 
-    w = ics.WORKLOADS[WORKLOAD]
+    if args.workload == ics.ENSEMBLE["name"]:
+        return run_ensemble(args, ws, rank, local)
+    if args.workload not in ics.WORKLOADS:
+        raise SystemExit(f"unknown workload {args.workload}")
+    w = ics.WORKLOADS[args.workload]
     N, cic, dt = w["N"], w["cic"], w["dt"]
     P = args.particles or w["P"]
-    state = ics.make_workload(WORKLOAD, P)
-    config = {"workload": WORKLOAD, "particles": P, "lattice": N, "deposit": "CIC" if cic else "NGP", "dt": dt,
-              "ic": "exponential disk, scale 200 cells, v_c from enclosed mass + 5% dispersion, lognormal(0,0.3) masses",
-              "l2": "particle state (20 B/particle = 400 MB) exceeds the 126 MB L2 every step; the lattice "
-                    "fields (~70 MB) stay L2-resident by design"}
+    state = ics.make_workload(args.workload, P)
+    config = {"workload": args.workload, "particles": P, "lattice": N, "deposit": "CIC" if cic else "NGP", "dt": dt,
+              "ic": IC_TEXT[args.workload],
+              "l2": f"particle state ({20 * P / 1e6:.0f} MB at 20 B/particle) and lattice fields "
+                    f"({70 * N * N / 2048 ** 2:.0f} MB) against the 126 MB L2"}
 
     if args.impl == "reference":
         if rank != 0:

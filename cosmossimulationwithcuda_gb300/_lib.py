@@ -31,6 +31,10 @@ EXPORTS = (
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
     "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
     "cosmos_pm_host_alloc", "cosmos_pm_host_free",
+    "cosmos_ensemble_default_config", "cosmos_ensemble_create", "cosmos_ensemble_destroy",
+    "cosmos_ensemble_set_particles", "cosmos_ensemble_get_particles", "cosmos_ensemble_step",
+    "cosmos_ensemble_synchronize", "cosmos_ensemble_get_field", "cosmos_ensemble_launches_per_step",
+    "cosmos_ensemble_stream", "cosmos_ensemble_last_error",
 )
 NOALLOC_MAX_PARTICLES = 1 << 20
 
@@ -49,6 +53,20 @@ class Config(ctypes.Structure):
         ("use_graph", ctypes.c_int32),
         ("blur_r", ctypes.c_int32),
         ("reserved", ctypes.c_int32 * 6),
+    ]
+
+
+class EnsembleConfig(ctypes.Structure):
+    _fields_ = [
+        ("num_sims", ctypes.c_int32),
+        ("deposit", ctypes.c_int32),
+        ("dt", ctypes.c_float),
+        ("gravity_multiplier", ctypes.c_float),
+        ("device", ctypes.c_int32),
+        ("force_mode", ctypes.c_int32),
+        ("sort_interval", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 8),
     ]
 
 
@@ -104,6 +122,18 @@ def load(path: str | None = None):
         "cosmos_pm_get_frame_async": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(ctypes.c_uint64)]),
         "cosmos_pm_host_alloc": (ctypes.c_int, [i64, ctypes.POINTER(_vp)]),
         "cosmos_pm_host_free": (ctypes.c_int, [_vp]),
+        "cosmos_ensemble_default_config": (None, [ctypes.POINTER(EnsembleConfig)]),
+        "cosmos_ensemble_create": (ctypes.c_int, [ctypes.POINTER(EnsembleConfig), ctypes.POINTER(i32),
+                                                  ctypes.POINTER(i64), ctypes.POINTER(_vp)]),
+        "cosmos_ensemble_destroy": (ctypes.c_int, [_vp]),
+        "cosmos_ensemble_set_particles": (ctypes.c_int, [_vp, i32, _f32p, _f32p, _f32p, _f32p, _f32p, i64, i64]),
+        "cosmos_ensemble_get_particles": (ctypes.c_int, [_vp, i32, _f32p, _f32p, _f32p, _f32p, _f32p, i64, i64]),
+        "cosmos_ensemble_step": (ctypes.c_int, [_vp, i32]),
+        "cosmos_ensemble_synchronize": (ctypes.c_int, [_vp]),
+        "cosmos_ensemble_get_field": (ctypes.c_int, [_vp, i32, i32, _f32p]),
+        "cosmos_ensemble_launches_per_step": (ctypes.c_int, [_vp, ctypes.POINTER(i32)]),
+        "cosmos_ensemble_stream": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64)]),
+        "cosmos_ensemble_last_error": (ctypes.c_char_p, [_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -272,3 +302,93 @@ class Simulation:
 
 def version() -> str:
     return load().cosmos_pm_version().decode()
+
+
+class Ensemble:
+    """Many independent simulations stepped together (include/cosmos_ensemble.h).
+
+    lattice_n[s], num_particles[s] per simulation (P_s a multiple of 4); one
+    dt, deposit, gravity multiplier and force mode for all."""
+
+    def __init__(self, lattice_n, num_particles, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0,
+                 device: int = 0, force_mode: int = FORCE_SPECTRAL, sort_interval: int = 32, use_graph: bool = True):
+        self.L = load()
+        ns = np.ascontiguousarray(lattice_n, np.int32)
+        ps = np.ascontiguousarray(num_particles, np.int64)
+        if ns.shape != ps.shape or ns.ndim != 1:
+            raise ValueError("lattice_n and num_particles must be 1-D of equal length")
+        cfg = EnsembleConfig()
+        self.L.cosmos_ensemble_default_config(ctypes.byref(cfg))
+        cfg.num_sims = ns.size
+        cfg.deposit = DEPOSIT_CIC if cic else DEPOSIT_NGP
+        cfg.dt = dt
+        cfg.gravity_multiplier = gravity_multiplier
+        cfg.device = device
+        cfg.force_mode = force_mode
+        cfg.sort_interval = sort_interval
+        cfg.use_graph = int(use_graph)
+        self.cfg = cfg
+        h = _vp()
+        rc = self.L.cosmos_ensemble_create(ctypes.byref(cfg), ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                           ps.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), ctypes.byref(h))
+        if rc != COSMOS_OK:
+            raise CosmosError(rc, self.L.cosmos_ensemble_last_error(None).decode())
+        self.h = h
+        self.N = [int(n) for n in ns]
+        self.P = [int(p) for p in ps]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cosmos_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != COSMOS_OK:
+            raise CosmosError(rc, self.L.cosmos_ensemble_last_error(self.h).decode())
+
+    def set_particles(self, sim: int, x, y, x_old=None, y_old=None, m=None, offset: int = 0):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (x, y, x_old, y_old, m)]
+        self._check(self.L.cosmos_ensemble_set_particles(self.h, sim, *[_ptr(a) for a in arrs], arrs[0].size, offset))
+
+    def set_state(self, sim: int, s):
+        self.set_particles(sim, s.x, s.y, s.x_old, s.y_old, s.m)
+
+    def get_particles(self, sim: int, count: int | None = None, offset: int = 0):
+        count = self.P[sim] - offset if count is None else count
+        out = [np.empty(count, np.float32) for _ in range(5)]
+        self._check(self.L.cosmos_ensemble_get_particles(self.h, sim, *[_ptr(a) for a in out], count, offset))
+        return out
+
+    def step(self, n: int = 1):
+        self._check(self.L.cosmos_ensemble_step(self.h, n))
+
+    def synchronize(self):
+        self._check(self.L.cosmos_ensemble_synchronize(self.h))
+
+    def get_field(self, sim: int, field: int):
+        N = self.N[sim]
+        out = np.empty((N, N, 2) if field == FIELD_FORCE else (N, N), np.float32)
+        self._check(self.L.cosmos_ensemble_get_field(self.h, sim, field, _ptr(out)))
+        return out
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int32()
+        self._check(self.L.cosmos_ensemble_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+    def stream(self) -> int:
+        s = ctypes.c_uint64()
+        self._check(self.L.cosmos_ensemble_stream(self.h, ctypes.byref(s)))
+        return s.value

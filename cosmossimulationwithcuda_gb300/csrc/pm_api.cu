@@ -4,8 +4,9 @@
 //
 // Stands in for the Universe<K> class of CosmosCuda.cuh (constructor
 // :881-1035, clear :1038-1069, step methods :1209-1300, worker loop
-// :1318-1364, destructor :1396-1427).  The reference's multi-GPU exchange,
-// render chain and frame ring are not part of this path.
+// :1318-1364, destructor :1396-1427) and its render chain (:1249-1256, kernels
+// in pm_render.cu).  The frame ring and worker thread live in the C++ drop-in
+// header (include/CosmosGB300.cuh); the multi-GPU exchange is not built.
 #include <cmath>
 #include <cstring>
 #include <deque>
@@ -441,7 +442,8 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
     const int ntiles = (N >> h->gran) * (N >> h->gran);
     h->max_items = cpm::max_work_items(h->Pq, ntiles);
     if (rc == COSMOS_OK) {
-        if ((rc = dalloc(&h->tstart, size_t(ntiles))) || (rc = dalloc(&h->tend, size_t(ntiles))) ||
+        const size_t nranges = cpm::tile_range_elems(N, h->gran, 1);
+        if ((rc = dalloc(&h->tstart, nranges)) || (rc = dalloc(&h->tend, nranges)) ||
             (rc = dalloc(&h->items, h->max_items)) || (rc = dalloc(&h->n_items, 1)))
             ;
     }

@@ -23,6 +23,10 @@
 //  3. k_rows_c2r   : B rows per CTA, Hermitian pre-split + N/2-point inverse
 //                    FFT, the potential row written as float2 pairs.
 // The filter build runs passes 1-2 in FP64 on the Green's lattice.
+//
+// Batches: every pass takes gridDim.y independent lattices of the same N
+// stored back to back (an ensemble of simulations); blockIdx.y selects the
+// lattice, and the filter K and the twiddles are shared.
 #include <cmath>
 #include <vector>
 
@@ -77,6 +81,8 @@ __global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_r2c(const T* 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
     const int y0 = int(blockIdx.x) * B;
+    in += size_t(blockIdx.y) * N * N;
+    spec += size_t(blockIdx.y) * M * N;
     // Row b as M complex values z[n] = (x[2n], x[2n+1]).
     const C* rows = reinterpret_cast<const C*>(in + size_t(y0) * N);
     auto src = [rows](int line, int i) { return rows[line * M + i]; };
@@ -111,7 +117,7 @@ __global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_cols_conv(float2* 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
     const int kx0 = int(blockIdx.x) * B;
-    C* lines = spec + size_t(kx0) * N;
+    C* lines = spec + size_t(blockIdx.y) * M * N + size_t(kx0) * N;
     auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
     auto gstore = [lines](int line, int i, C v) { lines[size_t(line) * N + i] = v; };
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
@@ -217,6 +223,8 @@ __global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_c2r(const flo
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
     const int y0 = int(blockIdx.x) * B;
+    spec += size_t(blockIdx.y) * M * STRIDE;              // M lines of STRIDE per lattice
+    out += size_t(blockIdx.y) * gridDim.x * B * N;        // gridDim.x * B rows per lattice
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
         const int b = idx - k * B;
@@ -291,6 +299,9 @@ __global__ void __launch_bounds__(NT, 3) k_cols_spectral(float2* __restrict__ sp
     C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): phi_hat; [B, 2B): phi_hat * iS
     float* red = reinterpret_cast<float*>(s + 2 * B * LP);
     const int kx0 = int(blockIdx.x) * B;
+    spec += size_t(blockIdx.y) * M * N;
+    spec2 += size_t(blockIdx.y) * M * N;
+    edge += size_t(blockIdx.y) * M * 4;
     C* lines = spec + size_t(kx0) * N;
     auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
@@ -363,6 +374,9 @@ __global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __res
     float* red = reinterpret_cast<float*>(s + 2 * B * LP);
     __shared__ float dx[B][3];
     const int y0 = int(blockIdx.x) * B;
+    spec += size_t(blockIdx.y) * M * N;
+    spec2 += size_t(blockIdx.y) * M * N;
+    force += size_t(blockIdx.y) * M * N;  // float4 = two cells
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
         const int b = idx - k * B;
@@ -431,6 +445,8 @@ __global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __res
 __global__ void k_apply_edge_rows(const float* __restrict__ dy, float2* __restrict__ force, int N, float g) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= N) return;
+    dy += size_t(blockIdx.y) * 3 * N;
+    force += size_t(blockIdx.y) * N * N;
     const float c12 = g * (1.0f / 12.0f);
     const float d01 = dy[x], d02 = dy[N + x], d13 = dy[2 * N + x];
     force[x].y += (-8.0f * d01 + d02) * c12;
@@ -474,12 +490,12 @@ static cudaError_t allow_smem(K kernel, size_t bytes) {
 
 template <int N>
 static cudaError_t conv_passes_n(const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                                 cudaStream_t st) {
+                                 int batch, cudaStream_t st) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
-    k_rows_r2c<float, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(rho, spec, tw);
-    k_cols_conv<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, CS::smem, st>>>(spec, kq, tw);
-    k_rows_c2r<N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(spec, phi, tw);
+    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_cols_conv<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, CS::smem, st>>>(spec, kq, tw);
+    k_rows_c2r<N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(spec, phi, tw);
     return cudaGetLastError();
 }
 
@@ -524,22 +540,23 @@ struct SpecShape {
 // with events, which CUDA-graph capture records as graph edges).
 template <int N>
 static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                     const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                     cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
+                                     const float* kq, float2* force, const float2* tw, float g, int batch,
+                                     cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
     cudaError_t e;
-    k_rows_r2c<float, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(rho, spec, tw);
-    k_cols_spectral<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, SS::col_smem, st>>>(spec, spec2, edge, kq, tw, g);
+    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_cols_spectral<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, SS::col_smem, st>>>(spec, spec2, edge,
+                                                                                                    kq, tw, g);
     if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
-    k_rows_c2r<N, 1, SS::ENT, 4><<<3, SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
+    k_rows_c2r<N, 1, SS::ENT, 4><<<dim3(3, batch), SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
     if ((e = cudaEventRecord(join, aux)) != cudaSuccess) return e;
-    k_rows_c2r_spectral<N, SS::RB, SS::RNT><<<N / SS::RB, SS::RNT, SS::row_smem, st>>>(
+    k_rows_c2r_spectral<N, SS::RB, SS::RNT><<<dim3(N / SS::RB, batch), SS::RNT, SS::row_smem, st>>>(
         spec, spec2, reinterpret_cast<float4*>(force), tw, g);
     if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
-    k_apply_edge_rows<<<(N + 255) / 256, 256, 0, st>>>(dy, force, N, g);
+    k_apply_edge_rows<<<dim3((N + 255) / 256, batch), 256, 0, st>>>(dy, force, N, g);
     return cudaGetLastError();
 }
 
@@ -567,11 +584,12 @@ cudaError_t prepare_spectral_passes(int N) {
 
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch) {
+    if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, st, aux, fork, join);
+        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:
@@ -606,11 +624,12 @@ cudaError_t prepare_conv_passes(int N) {
 }
 
 cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                               cudaStream_t st) {
+                               cudaStream_t st, int batch) {
+    if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return conv_passes_n<n>(rho, spec, kq, phi, tw, st);
+        return conv_passes_n<n>(rho, spec, kq, phi, tw, batch, st);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:

@@ -8,8 +8,9 @@ namespace cpm {
 
 // pm_fft.cu
 cudaError_t prepare_conv_passes(int N);
+// batch: lattices of size N stored back to back, processed in one launch per pass
 cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                               cudaStream_t st);
+                               cudaStream_t st, int batch = 1);
 int conv_launches_per_step();
 int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st);
 // Spectral force: density -> force field (interleaved fx, fy) with the
@@ -19,7 +20,7 @@ cudaError_t prepare_spectral_passes(int N);
 // aux/fork/join: an auxiliary stream and two events for the concurrent edge pass.
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join);
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1);
 int spectral_launches_per_step();
 
 // pm_particles.cu
@@ -34,11 +35,14 @@ struct ParticleArrays {
 
 cudaError_t launch_deposit_global(const ParticleArrays& p, int64_t P, float* rho, int N, int cic, int nsm,
                                   cudaStream_t st);
-cudaError_t launch_gradient(const float* phi, float2* force, int N, float gmult, cudaStream_t st);
+cudaError_t launch_gradient(const float* phi, float2* force, int N, float gmult, cudaStream_t st, int batch = 1);
 cudaError_t launch_integrate(const float2* force, const ParticleArrays& p, int64_t P, int N, int cic, float dt,
                              int nsm, cudaStream_t st);
 cudaError_t launch_tile_keys(const float* x, const float* y, int64_t P, int N, int gran, uint32_t* keys,
                              cudaStream_t st);
+// Ensemble keys: sim * (T^2 + 1) + tile key, slots [sim_off[s], sim_off[s+1]) in sim s.
+cudaError_t launch_tile_keys_sims(const float* x, const float* y, int64_t P, int N, int gran, const int64_t* sim_off,
+                                  int nsims, uint32_t* keys, cudaStream_t st);
 
 // Stable LSD radix sort of (key, value) pairs on the low `bits` bits of the key.
 struct RadixScratch {
@@ -82,8 +86,10 @@ struct WorkItem {
     float scale;          // fixed-point scale of the deposit window (a power of two)
     float inv_scale;      // 1 / scale
     float heavy;          // particles heavier than this deposit with global float atomics
-    uint32_t pad;
+    uint32_t sim;         // lattice index within an ensemble (0 for one simulation)
 };
+// Elements of the tile-range arrays (tstart / tend) for nsims simulations.
+size_t tile_range_elems(int N, int gran, int nsims);
 size_t tile_window_smem(int gran);
 size_t max_work_items(int64_t Pq, int ntiles);
 cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid);
@@ -91,7 +97,7 @@ cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid);
 // masses of the sorted particles are read from `m`).
 cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
                                uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
-                               cudaStream_t st);
+                               cudaStream_t st, int nsims = 1);
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
                                cudaStream_t st);

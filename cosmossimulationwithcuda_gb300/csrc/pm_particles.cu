@@ -77,6 +77,8 @@ cudaError_t launch_deposit_global(const ParticleArrays& p, int64_t P, float* rho
 __global__ void __launch_bounds__(kThreads) k_gradient(const float* __restrict__ phi, float2* __restrict__ force,
                                                        int N, int logN, float gmult) {
     const int64_t NN = int64_t(N) * N;
+    phi += size_t(blockIdx.y) * NN;  // batch of lattices back to back
+    force += size_t(blockIdx.y) * NN;
     for (int64_t idx = blockIdx.x * int64_t(kThreads) + threadIdx.x; idx < NN; idx += int64_t(gridDim.x) * kThreads) {
         const int cx = int(idx & (N - 1));
         const int cy = int(idx >> logN);
@@ -93,11 +95,13 @@ __global__ void __launch_bounds__(kThreads) k_gradient(const float* __restrict__
     }
 }
 
-cudaError_t launch_gradient(const float* phi, float2* force, int N, float gmult, cudaStream_t st) {
+cudaError_t launch_gradient(const float* phi, float2* force, int N, float gmult, cudaStream_t st, int batch) {
+    if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     const int64_t NN = int64_t(N) * N;
     int grid = int((NN + kThreads - 1) / kThreads);
-    if (grid > 152 * 8) grid = 152 * 8;
-    k_gradient<<<grid, kThreads, 0, st>>>(phi, force, N, ilog2(N), gmult);
+    const int cap = (152 * 8 + batch - 1) / batch;
+    if (grid > cap) grid = cap;
+    k_gradient<<<dim3(grid, batch), kThreads, 0, st>>>(phi, force, N, ilog2(N), gmult);
     return cudaGetLastError();
 }
 
@@ -158,6 +162,32 @@ __global__ void __launch_bounds__(kThreads) k_tile_keys(const float* __restrict_
 cudaError_t launch_tile_keys(const float* x, const float* y, int64_t P, int N, int gran, uint32_t* keys,
                              cudaStream_t st) {
     if (P > 0) k_tile_keys<<<stream_grid(P, 152), kThreads, 0, st>>>(x, y, P, N, gran, keys);
+    return cudaGetLastError();
+}
+
+// Ensemble keys: slots [sim_off[s], sim_off[s+1]) belong to simulation s; the
+// key is s * (T^2 + 1) + the tile key (T^2 = inactive), so one sort orders
+// every simulation's segment by tile and keeps the segments in place.
+__global__ void __launch_bounds__(kThreads) k_tile_keys_sims(const float* __restrict__ x, const float* __restrict__ y,
+                                                             int64_t P, int N, int gran,
+                                                             const int64_t* __restrict__ sim_off, int nsims,
+                                                             uint32_t* __restrict__ keys) {
+    const uint32_t T = uint32_t(N >> gran);
+    const uint32_t stride = T * T + 1u;
+    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < P; i += int64_t(gridDim.x) * kThreads) {
+        int lo = 0, hi = nsims;  // largest s with sim_off[s] <= i
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(sim_off + mid) <= i) lo = mid; else hi = mid;
+        }
+        keys[i] = uint32_t(lo) * stride + tile_key(__ldg(x + i), __ldg(y + i), N, gran);
+    }
+}
+
+cudaError_t launch_tile_keys_sims(const float* x, const float* y, int64_t P, int N, int gran, const int64_t* sim_off,
+                                  int nsims, uint32_t* keys, cudaStream_t st) {
+    if (P > 0 && nsims > 0)
+        k_tile_keys_sims<<<stream_grid(P, 152), kThreads, 0, st>>>(x, y, P, N, gran, sim_off, nsims, keys);
     return cudaGetLastError();
 }
 

@@ -174,16 +174,20 @@ __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, int64_t n, uint
 }
 
 // One CTA: count the items of each tile, scan, write the items (tile order).
+// Keys run over nsims blocks of `stride` = T^2 + 1 (the last one of each block
+// holds the inactive particles, which get no items); the simulation index goes
+// into WorkItem::sim.
 __global__ void __launch_bounds__(1024) k_build_items(const uint32_t* __restrict__ tstart,
-                                                      const uint32_t* __restrict__ tend, int ntiles, int gran,
-                                                      int item_max, WorkItem* __restrict__ items,
+                                                      const uint32_t* __restrict__ tend, int ntiles, int stride,
+                                                      int gran, int item_max, WorkItem* __restrict__ items,
                                                       uint32_t* __restrict__ n_items) {
     __shared__ uint32_t part[1024];
     const int seg = (ntiles + 1023) / 1024;
     const int lo = int(threadIdx.x) * seg;
     const int hi = min(lo + seg, ntiles);
     uint32_t cnt = 0;
-    for (int t = lo; t < hi; ++t) cnt += (tend[t] - tstart[t] + item_max - 1) / item_max;
+    for (int t = lo; t < hi; ++t)
+        if (t % stride != stride - 1) cnt += (tend[t] - tstart[t] + item_max - 1) / item_max;
     part[threadIdx.x] = cnt;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {
@@ -194,10 +198,12 @@ __global__ void __launch_bounds__(1024) k_build_items(const uint32_t* __restrict
     }
     uint32_t base = part[threadIdx.x] - cnt;
     for (int t = lo; t < hi; ++t) {
+        const int sim = t / stride, local = t - sim * stride;
+        if (local == stride - 1) continue;  // inactive particles
         const uint32_t s = tstart[t], c = tend[t] - s;
         const uint32_t nch = (c + item_max - 1) / item_max;
-        const int x0 = int(compact_bits(uint32_t(t)) << gran) - kTileHalo;
-        const int y0 = int(compact_bits(uint32_t(t) >> 1) << gran) - kTileHalo;
+        const int x0 = int(compact_bits(uint32_t(local)) << gran) - kTileHalo;
+        const int y0 = int(compact_bits(uint32_t(local) >> 1) << gran) - kTileHalo;
         for (uint32_t j = 0; j < nch; ++j) {
             WorkItem w;
             w.x0 = x0;
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(1024) k_build_items(const uint32_t* __restrict
             w.scale = 1.0f;
             w.inv_scale = 1.0f;
             w.heavy = FLT_MAX;
-            w.pad = 0;
+            w.sim = uint32_t(sim);
             items[base++] = w;
         }
     }
@@ -268,8 +274,12 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_tiles(const WorkItem* _
     float2* fwin = reinterpret_cast<float2*>(smem4);
     uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
     const uint32_t n_items = *n_items_p;
+    const float2* const force0 = force;
+    float* const rho0 = rho;
     for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
         const WorkItem item = items[it];
+        force = force0 + size_t(item.sim) * N * N;  // the item's lattice (ensembles)
+        rho = rho0 + size_t(item.sim) * N * N;
         if (item.end - item.begin < uint32_t(kItemDirect)) {
             // sparse tile: no windows, global gathers and atomics
             const Window w{nullptr, nullptr, item.x0, item.y0, 1.0f, 0.0f};
@@ -358,11 +368,17 @@ cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid) {
     return e;
 }
 
+size_t tile_range_elems(int N, int gran, int nsims) {
+    const size_t t = size_t(N >> gran);
+    return (t * t + 1) * size_t(nsims);
+}
+
 cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
                                uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
-                               cudaStream_t st) {
+                               cudaStream_t st, int nsims) {
     const int t = N >> gran;
-    const uint32_t ntiles = uint32_t(t) * uint32_t(t);
+    const int stride = t * t + 1;
+    const uint32_t ntiles = uint32_t(tile_range_elems(N, gran, nsims));
     cudaError_t e = cudaMemsetAsync(tstart, 0, ntiles * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(tend, 0, ntiles * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
@@ -371,7 +387,7 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
         if (g > 4096) g = 4096;
         k_tile_ranges<<<int(g), 256, 0, st>>>(sorted_keys, Pq, ntiles, tstart, tend);
     }
-    k_build_items<<<1, 1024, 0, st>>>(tstart, tend, int(ntiles), gran, kItemMax, items, n_items);
+    k_build_items<<<1, 1024, 0, st>>>(tstart, tend, int(ntiles), stride, gran, kItemMax, items, n_items);
     if (max_items > 0) k_item_scales<<<unsigned(max_items), 256, 0, st>>>(m, items, n_items);
     return cudaGetLastError();
 }

@@ -217,6 +217,32 @@ WORKLOADS = {
 }
 
 
+# The 64-simulation ensemble: N uniform over {256, 512, 1024}, P log-uniform
+# over [1e4, 2e6] (rounded to a multiple of 4), initial conditions alternating
+# between a binary (two Plummer spheres, 1 : 0.6, circular orbit) and an
+# exponential disk; CIC, dt = 0.002.
+ENSEMBLE = dict(name="ensemble-64-mixed-cic", sims=64, lattices=(256, 512, 1024), p_min=1e4, p_max=2e6,
+                cic=True, dt=0.002, steps=200)
+
+
+def ensemble_workload(seed: int = 4, sims: int | None = None, p_scale: float = 1.0):
+    """(lattice sizes, particle counts, states) of the ensemble workload."""
+    e = ENSEMBLE
+    sims = e["sims"] if sims is None else sims
+    rng = np.random.default_rng(seed)
+    Ns = rng.choice(np.array(e["lattices"]), sims)
+    Ps = np.exp(rng.uniform(np.log(e["p_min"]), np.log(e["p_max"]), sims)) * p_scale
+    Ps = np.maximum((np.round(Ps / 4) * 4).astype(np.int64), 4)
+    states = []
+    for i, (N, P) in enumerate(zip(Ns, Ps)):
+        N, P = int(N), int(P)
+        if i % 2 == 0:
+            states.append(binary_star(P, N, e["dt"], seed=1000 + i))
+        else:
+            states.append(exponential_disk(P, N, e["dt"], seed=1000 + i, scale=N / 10.0))
+    return [int(n) for n in Ns], [int(p) for p in Ps], states
+
+
 def make_workload(name: str, P: int | None = None, seed: int | None = None) -> ParticleState:
     w = WORKLOADS[name]
     P = w["P"] if P is None else P

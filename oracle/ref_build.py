@@ -29,6 +29,8 @@ CONFIGS = [
     (128, 0.005, 1.0),
     (512, 0.002, 1.0),
     (2048, 0.001, 1.0),
+    (4096, 0.001, 1.0),
+    (8192, 0.0005, 1.0),
 ]
 
 

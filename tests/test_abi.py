@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(cosmos_lib):
 
 
 def test_binding_covers_header(cosmos_lib):
-    assert set(cosmos_lib.EXPORTS) >= {n for n in _declared_functions() if n.startswith("cosmos_pm_")}
+    assert set(cosmos_lib.EXPORTS) >= {n for n in _declared_functions() if n.startswith(("cosmos_pm_", "cosmos_ensemble_"))}
 
 
 def test_version_and_default_config(cosmos_lib):
@@ -63,3 +63,8 @@ def test_universe_dropin_header_compiles():
                         "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cpp", "universe_test.cpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_ensemble_config_layout(cosmos_lib):
+    import ctypes as C
+    assert C.sizeof(cosmos_lib.EnsembleConfig) == 4 * 8 + 4 * 8  # matches cosmos_ensemble_config
