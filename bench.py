@@ -340,6 +340,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=20)
     ap.add_argument("--render-interval", type=int, default=2,
                     help="e2e: read the positions back every this many steps")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the sort granularity / cadence with cosmos_pm_autotune on this state first")
     ap.add_argument("--workload", default=WORKLOAD,
                     help="the headline disk (default), another single-simulation workload "
                          "(uniform-1M-512-ngp, collide-100M-4096-cic, clumpy-1B-8192-cic) or "
@@ -384,7 +386,19 @@ def main():
     rt = CudaRT()
     rt.lib.cudaSetDevice(local)
     mode = _lib.FORCE_SPECTRAL if args.force_mode == "spectral" else _lib.FORCE_GRADIENT
-    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=args.sort_interval, force_mode=mode)
+    sort_interval, sort_gran = args.sort_interval, -1
+    if args.autotune:
+        cache = os.environ.get("COSMOS_PM_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "cosmos_pm",
+                                                                     "autotune.txt"))
+        os.makedirs(os.path.dirname(cache), exist_ok=True)
+        t0 = time.perf_counter()
+        g, itv, tms = _lib.autotune(state, N, cic=cic, dt=dt, device=local, force_mode=mode, steps=128,
+                                    cache_path=cache)
+        sort_interval, sort_gran = itv, (g if itv else -1)
+        config["autotune"] = {"sort_granularity": g, "sort_interval": itv, "ms_per_step": tms,
+                              "search_s": round(time.perf_counter() - t0, 2), "cache": cache}
+    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=sort_interval, force_mode=mode,
+                          sort_granularity=sort_gran)
     stream = sim.stream()
     sim.set_state(state)
     config["force_mode"] = args.force_mode
@@ -398,6 +412,16 @@ def main():
         sim.run_stage(_lib.STAGE_FORCE)
         force_err = force_error_vs_fp64(state, N, cic, dt, sim.get_field(_lib.FIELD_FORCE))
         sim.set_state(state)  # the stage hooks leave the state untouched; restart cleanly
+
+    # ---- FP64 energy / momentum before the run (outside the timed region) ----
+    def conserved():
+        sim.run_stage(_lib.STAGE_DEPOSIT)
+        sim.run_stage(_lib.STAGE_POTENTIAL)
+        ke, pe, px, py = sim.diagnostics()
+        # force = +grad(phi) with phi = G * rho > 0: E = KE - sum(m phi)/2
+        return {"kinetic": ke, "potential": -pe, "energy": ke - pe, "momentum": [px, py]}
+
+    cons0 = conserved()
 
     # ---- device-timed throughput (state resident) ----
     clk = ClockSampler(local).__enter__()
@@ -424,6 +448,15 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = P * args.steps * ws / (ms / 1e3)
+    cons1 = conserved()
+    mtot = float(np.sum(state.m, dtype=np.float64))
+    # momentum scale ~ sum m|v| (the larger kinetic energy: runs may start at rest)
+    pscale = float(np.sqrt(2.0 * mtot * max(cons0["kinetic"], cons1["kinetic"], 1e-300)))
+    drift = {"steps": args.warmup + args.steps, "start": cons0, "end": cons1,
+             "energy_rel": (cons1["energy"] - cons0["energy"]) / abs(cons0["energy"]) if cons0["energy"] else None,
+             "momentum_rel": float(np.hypot(cons1["momentum"][0] - cons0["momentum"][0],
+                                            cons1["momentum"][1] - cons0["momentum"][1]) / pscale),
+             "note": "FP64 sums on the GPU over active particles; v = (x - xOld)/dt, phi sampled at the NGP cell"}
 
     # ---- per-stage times (profiled direct launches, events between kernels) ----
     sim.set_profiling(True)
@@ -519,7 +552,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches, "stages_ms": stages, "reference_gpu": ref_gpu,
-            "force_rel_err_vs_fp64": force_err}
+            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift}
     print(json.dumps(line), flush=True)
 
 

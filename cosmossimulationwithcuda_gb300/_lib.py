@@ -30,7 +30,7 @@ EXPORTS = (
     "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
     "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
-    "cosmos_pm_host_alloc", "cosmos_pm_host_free",
+    "cosmos_pm_host_alloc", "cosmos_pm_host_free", "cosmos_pm_autotune",
     "cosmos_ensemble_default_config", "cosmos_ensemble_create", "cosmos_ensemble_destroy",
     "cosmos_ensemble_set_particles", "cosmos_ensemble_get_particles", "cosmos_ensemble_step",
     "cosmos_ensemble_synchronize", "cosmos_ensemble_get_field", "cosmos_ensemble_launches_per_step",
@@ -122,6 +122,8 @@ def load(path: str | None = None):
         "cosmos_pm_get_frame_async": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(ctypes.c_uint64)]),
         "cosmos_pm_host_alloc": (ctypes.c_int, [i64, ctypes.POINTER(_vp)]),
         "cosmos_pm_host_free": (ctypes.c_int, [_vp]),
+        "cosmos_pm_autotune": (ctypes.c_int, [ctypes.POINTER(Config), _f32p, _f32p, _f32p, _f32p, _f32p, i32,
+                                              ctypes.c_char_p, ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_float)]),
         "cosmos_ensemble_default_config": (None, [ctypes.POINTER(EnsembleConfig)]),
         "cosmos_ensemble_create": (ctypes.c_int, [ctypes.POINTER(EnsembleConfig), ctypes.POINTER(i32),
                                                   ctypes.POINTER(i64), ctypes.POINTER(_vp)]),
@@ -155,6 +157,24 @@ def default_config(**kw) -> Config:
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+def autotune(state, N: int, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0, device: int = 0,
+             force_mode: int = FORCE_SPECTRAL, steps: int = 128, cache_path: str | None = None):
+    """Fastest (sort_granularity, sort_interval) for this state, measured on the
+    device (cosmos_pm_autotune).  Returns (granularity, interval, ms_per_step)."""
+    L = load()
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (state.x, state.y, state.x_old, state.y_old, state.m)]
+    base = default_config(lattice_n=N, deposit=DEPOSIT_CIC if cic else DEPOSIT_NGP, dt=dt,
+                          gravity_multiplier=gravity_multiplier, num_particles=arrs[0].size, device=device,
+                          force_mode=force_mode)
+    best = Config()
+    ms = ctypes.c_float()
+    rc = L.cosmos_pm_autotune(ctypes.byref(base), *[_ptr(a) for a in arrs], steps,
+                              cache_path.encode() if cache_path else None, ctypes.byref(best), ctypes.byref(ms))
+    if rc != COSMOS_OK:
+        raise CosmosError(rc, L.cosmos_pm_last_error(None).decode())
+    return best.sort_granularity, best.sort_interval, ms.value
 
 
 class Simulation:

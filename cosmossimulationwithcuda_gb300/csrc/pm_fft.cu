@@ -41,6 +41,8 @@ namespace cpm {
 // per row CTA (at least 4 rows, so that the transposed spectrum moves in
 // 32-byte sectors) and one 2048-point line per column CTA, so that 4-6 CTAs
 // are resident per SM and their load / transform / store phases overlap.
+// Below 2048^2 the rows and lines per CTA shrink so that one lattice still
+// spreads over at least 128 CTAs (N/128 rows, N/256 lines).
 // FP64 (filter build) halves the rows to keep shared memory in range.
 constexpr int kMaxRadix = 16;
 constexpr int ceil_pow2_min(int v, int lo) { return v < lo ? lo : v; }
@@ -49,7 +51,8 @@ constexpr int clamp_threads(int v) { return v < 64 ? 64 : (v > 1024 ? 1024 : v);
 template <class T, int N>
 struct RowShape {
     static constexpr int M = N / 2;
-    static constexpr int Bf0 = ceil_pow2_min(4096 / M, 4);
+    static constexpr int Bw = 4096 / M < N / 128 ? 4096 / M : N / 128;  // work per CTA vs CTA count
+    static constexpr int Bf0 = ceil_pow2_min(Bw, 4);
     static constexpr int Bf = Bf0 > N ? N : Bf0;
     static constexpr int B = (sizeof(T) == 8 && Bf > 1) ? (Bf / 2) : Bf;  // rows per CTA
     static constexpr int NT = clamp_threads(B * M / kMaxRadix);
@@ -59,7 +62,8 @@ struct RowShape {
 template <class T, int N>
 struct ColShape {
     static constexpr int M = N / 2;
-    static constexpr int B0 = ceil_pow2_min(2048 / N, 1);
+    static constexpr int Bw = 2048 / N < M / 128 ? 2048 / N : M / 128;
+    static constexpr int B0 = ceil_pow2_min(Bw, 1);
     static constexpr int B = B0 > M ? M : B0;  // lines per CTA
     static constexpr int NT = clamp_threads(B * N / kMaxRadix);
     static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);

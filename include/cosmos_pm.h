@@ -185,9 +185,11 @@ int cosmos_pm_diagnostics(cosmos_pm* h, double* kinetic, double* potential, doub
                           double* momentum_y);
 
 /* Per-stage device time of the last step run with profiling on (ms), for
- * benchmarks.  times[i] in the order deposit, fft-rows, fft-columns,
- * fft-inverse-rows, force, integrate, sort; n = capacity.  Returns the number
- * of entries written in *n. */
+ * benchmarks: times[i] in the order prologue deposit (first step after the
+ * state was written, else 0), FFT passes (spectral mode: all force passes),
+ * stencil (gradient mode), fused gather + update + deposit, tile sort (0 when
+ * the step did not sort).  Profiled steps run as direct launches with events
+ * between the stages.  *n = capacity on entry, entries written on return. */
 int cosmos_pm_set_profiling(cosmos_pm* h, int32_t enabled);
 int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n);
 
@@ -197,6 +199,23 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream);
 
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
+
+/* ---- autotuning -----------------------------------------------------------
+ * No counterpart in the reference (its launch shapes are compile-time
+ * constants, CosmosCuda.cuh:29-74).  Searches the tile edge of the particle
+ * sort (sort_granularity 4, 5, 6: 16, 32, 64 cells) and the re-sort cadence
+ * (sort_interval 8, 16, 32, 64, or never) on the caller's own particle state:
+ * each candidate runs on a temporary handle from the same host state, `steps`
+ * graph-launched steps timed with CUDA events after a warm-up that includes
+ * its first sort.  *best = *base with the fastest sort_granularity and
+ * sort_interval; *best_ms = its time per step (amortising the sorts).
+ * cache_path (may be NULL): a text file of earlier results keyed by lattice
+ * size, particle count (half-octave bucket), deposit, force mode and GPU
+ * name; a hit returns the cached choice without running, a miss appends the
+ * new result.  The handle memory of one candidate at a time is allocated. */
+int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, const float* y, const float* x_old,
+                       const float* y_old, const float* m, int32_t steps, const char* cache_path,
+                       cosmos_pm_config* best, float* best_ms);
 
 /* ---- tile sort without device allocation ---------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
