@@ -450,13 +450,19 @@ __global__ void __launch_bounds__(kThreads) k_diagnostics(ParticleArrays p, int6
                                                           int N, float dt, double* __restrict__ out) {
     double ke = 0.0, pe = 0.0, mx = 0.0, my = 0.0;
     const double inv_dt = 1.0 / double(dt);
+    // The wrap moves x by N-4 but leaves xOld on the far side (the reference
+    // keeps the pre-step position, CosmosCuda.cuh:288-301), so x - xOld of a
+    // wrapped particle carries +-(N-4) from then on: take the displacement
+    // modulo the wrap period.
+    const double period = double(N) - 4.0, half = 0.5 * period;
+    auto unwrap = [period, half](double d) { return d > half ? d - period : (d < -half ? d + period : d); };
     for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < P; i += int64_t(gridDim.x) * kThreads) {
         const float x = p.x[i], y = p.y[i];
         const int cx = int(x), cy = int(y);
         if (!active_cell(cx, cy, N)) continue;
         const double m = p.m[i];
-        const double vx = (double(x) - double(p.xo[i])) * inv_dt;
-        const double vy = (double(y) - double(p.yo[i])) * inv_dt;
+        const double vx = unwrap(double(x) - double(p.xo[i])) * inv_dt;
+        const double vy = unwrap(double(y) - double(p.yo[i])) * inv_dt;
         ke += 0.5 * m * (vx * vx + vy * vy);
         pe += 0.5 * m * double(phi[size_t(cx) + size_t(cy) * N]);
         mx += m * vx;

@@ -178,9 +178,12 @@ int cosmos_pm_tile_keys(cosmos_pm* h, const float* x, const float* y, int64_t co
                         uint32_t* keys);
 
 /* FP64 diagnostics: kinetic energy sum(m v^2)/2 with v = (x - xOld)/dt, the
- * momentum sum(m v), over active particles, and the potential energy
- * sum(m phi(x))/2 sampled from the potential field of the last step (NGP
- * sample).  No counterpart in the reference. */
+ * displacement taken modulo the wrap period N-4 (a wrapped particle's xOld
+ * stays on the far side), the momentum sum(m v), over active particles, and
+ * sum(m phi(x))/2 sampled from the potential field (NGP sample; run
+ * COSMOS_STAGE_DEPOSIT and COSMOS_STAGE_POTENTIAL first for the current
+ * positions).  With force = +grad(phi), the total energy is kinetic minus
+ * that sum.  No counterpart in the reference. */
 int cosmos_pm_diagnostics(cosmos_pm* h, double* kinetic, double* potential, double* momentum_x,
                           double* momentum_y);
 

@@ -355,6 +355,23 @@ def test_diagnostics_fp64(cosmos_lib, rng):
     vx = (st.x.astype(np.float64) - st.x_old) / dt
     vy = (st.y.astype(np.float64) - st.y_old) / dt
     m = st.m.astype(np.float64)
+    assert np.abs(vx).max() * dt < (N - 4) / 2  # no wrapped particles in this state
     np.testing.assert_allclose(ke, 0.5 * np.sum(m * (vx ** 2 + vy ** 2)), rtol=1e-12)
     np.testing.assert_allclose(px, np.sum(m * vx), rtol=1e-9, atol=1e-9)
     np.testing.assert_allclose(py, np.sum(m * vy), rtol=1e-9, atol=1e-9)
+
+
+def test_diagnostics_unwraps_wrapped_particles(cosmos_lib):
+    """A particle just wrapped keeps xOld on the far side; its velocity is the
+    displacement modulo the wrap period N - 4."""
+    N, dt = 64, float(np.float32(0.01))
+    x = np.array([2.5, 30.0, 30.0, 30.0], np.float32)
+    xo = np.array([2.5 + (N - 4) - 0.001, 30.0, 30.0, 30.0], np.float32)  # moved -0.001 across the edge
+    y = np.full(4, 30.0, np.float32)
+    m = np.ones(4, np.float32)
+    with _sim(cosmos_lib, N, 4, True, dt=dt) as s:
+        s.set_particles(x, y, xo, y, m)
+        ke, pe, px, py = s.diagnostics()
+    d = (np.float64(x[0]) - np.float64(xo[0])) + (N - 4)
+    assert abs(px - d / dt) <= 1e-9 * abs(d / dt) + 1e-12
+    assert abs(ke - 0.5 * (d / dt) ** 2) <= 1e-9 * ke
