@@ -245,7 +245,8 @@ def run_ensemble(args, ws, rank, local):
     _build.build()
     rt = CudaRT()
     rt.lib.cudaSetDevice(local)
-    mode = _lib.FORCE_SPECTRAL if args.force_mode == "spectral" else _lib.FORCE_GRADIENT
+    mode = {"spectral": _lib.FORCE_SPECTRAL, "gradient": _lib.FORCE_GRADIENT, "tc-fp16": _lib.FORCE_SPECTRAL_TC_FP16,
+            "tc-bf16": _lib.FORCE_SPECTRAL_TC_BF16}[args.force_mode]
     ens = _lib.Ensemble(Ns, Ps, cic=e["cic"], dt=e["dt"], device=local, force_mode=mode,
                         sort_interval=args.sort_interval if args.sort_interval > 0 else 32)
     for i, st in enumerate(states):
@@ -333,8 +334,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-interval", type=int, default=-1)
-    ap.add_argument("--force-mode", choices=["spectral", "gradient"], default="spectral",
-                    help="spectral: force from the FFT (<=1e-5 vs FP64); gradient: the reference's FP32 stencil")
+    ap.add_argument("--force-mode", choices=["spectral", "gradient", "tc-fp16", "tc-bf16"], default="spectral",
+                    help="spectral: force from the FFT (<=1e-5 vs FP64); gradient: the reference's FP32 stencil; "
+                         "tc-fp16 / tc-bf16: spectral with the column FFTs on the tensor cores (split precision)")
     ap.add_argument("--no-force-check", action="store_true", help="skip the FP64 force-accuracy check")
     ap.add_argument("--no-reference-gpu", action="store_true", help="skip timing the reference's kernels")
     ap.add_argument("--ref-steps", type=int, default=20)
@@ -385,7 +387,8 @@ def main():
     _build.build()
     rt = CudaRT()
     rt.lib.cudaSetDevice(local)
-    mode = _lib.FORCE_SPECTRAL if args.force_mode == "spectral" else _lib.FORCE_GRADIENT
+    mode = {"spectral": _lib.FORCE_SPECTRAL, "gradient": _lib.FORCE_GRADIENT, "tc-fp16": _lib.FORCE_SPECTRAL_TC_FP16,
+            "tc-bf16": _lib.FORCE_SPECTRAL_TC_BF16}[args.force_mode]
     sort_interval, sort_gran = args.sort_interval, -1
     if args.autotune:
         cache = os.environ.get("COSMOS_PM_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "cosmos_pm",
@@ -481,7 +484,7 @@ def main():
         "fused_step": 36.0 * P + 16.0 * N * N,
         # gradient mode: r2c rows 4+4, columns 4+1+4 (real K on a quarter: 1 B/cell), c2r rows 4+4;
         # spectral mode (force straight from the FFT): r2c 4+4, columns 4+1+8, c2r 8+8
-        "fft_conv": (37.0 if args.force_mode == "spectral" else 25.0) * N * N,
+        "fft_conv": (37.0 if args.force_mode != "gradient" else 25.0) * N * N,
         "force": 12.0 * N * N,
     }
     dom = max(algo, key=lambda k: stages.get(k, 0.0))

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "libcosmos_pm.so")
 COSMOS_OK = 0
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "NOMEM", -4: "RANGE", -5: "TIMEOUT", -6: "STATE"}
 DEPOSIT_NGP, DEPOSIT_CIC = 0, 1
-FORCE_GRADIENT, FORCE_SPECTRAL = 0, 1
+FORCE_GRADIENT, FORCE_SPECTRAL, FORCE_SPECTRAL_TC_FP16, FORCE_SPECTRAL_TC_BF16 = 0, 1, 2, 3
 FIELD_DENSITY, FIELD_POTENTIAL, FIELD_FORCE = 0, 1, 2
 STAGE_DEPOSIT, STAGE_POTENTIAL, STAGE_FORCE, STAGE_INTEGRATE = 0, 1, 2, 3
 

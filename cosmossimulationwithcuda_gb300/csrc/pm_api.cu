@@ -58,6 +58,9 @@ struct cosmos_pm {
     float2* spec2 = nullptr;  // spectral mode: y-inverse of the Fy spectrum
     float2* edge = nullptr;   // spectral mode: y-edge differences per line kx
     float* dy = nullptr;      // spectral mode: y-edge differences per column x
+    void* tc_dft = nullptr;   // tensor-core modes: DFT matrix image
+    int* tc_status = nullptr; // tensor-core modes: MMA wait timeout flag
+    cpm::SpectralTc tc{};
     float* kq = nullptr;
     float2* tw = nullptr;
     double* diag = nullptr;
@@ -143,15 +146,27 @@ ParticleArrays& state(cosmos_pm* h) { return h->buf[h->cur]; }
 int sort_now(cosmos_pm* h);
 int issue_ticket(cosmos_pm* h, uint64_t* ticket);
 
+bool is_spectral(int mode) {
+    return mode == COSMOS_FORCE_SPECTRAL || mode == COSMOS_FORCE_SPECTRAL_TC_FP16 ||
+           mode == COSMOS_FORCE_SPECTRAL_TC_BF16;
+}
+bool is_tc(int mode) { return mode == COSMOS_FORCE_SPECTRAL_TC_FP16 || mode == COSMOS_FORCE_SPECTRAL_TC_BF16; }
+
+int launch_spectral(cosmos_pm* h, cudaStream_t st) {
+    CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
+                                        h->cfg.gravity_multiplier, st, h->aux_stream, h->fork_ev, h->join_ev, 1,
+                                        is_tc(h->cfg.force_mode) ? &h->tc : nullptr));
+    return COSMOS_OK;
+}
+
 // Density -> force field.  Gradient mode: FFT convolution to the potential,
 // then the reference's edge-clamped stencil.  Spectral mode: the stencil is
 // applied in Fourier space (no potential field is written).  The profiling
 // event between the two halves marks the start of the force pass.
 int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
-    if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
-        CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
-                                            g, st, h->aux_stream, h->fork_ev, h->join_ev));
+    if (is_spectral(h->cfg.force_mode)) {
+        CPM_TRY(launch_spectral(h, st));
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
@@ -322,6 +337,8 @@ void destroy_all(cosmos_pm* h) {
     cudaFree(h->spec2);
     cudaFree(h->edge);
     cudaFree(h->dy);
+    cudaFree(h->tc_dft);
+    cudaFree(h->tc_status);
     cudaFree(h->kq);
     cudaFree(h->tw);
     cudaFree(h->diag);
@@ -372,8 +389,10 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return cpm::fail(COSMOS_ERR_INVALID, "num_particles must be in [0, 2^32 - 16]");
     if (!std::isfinite(cfg->dt) || !std::isfinite(cfg->gravity_multiplier))
         return cpm::fail(COSMOS_ERR_INVALID, "dt and gravity_multiplier must be finite");
-    if (cfg->force_mode != COSMOS_FORCE_GRADIENT && cfg->force_mode != COSMOS_FORCE_SPECTRAL)
-        return cpm::fail(COSMOS_ERR_INVALID, "force_mode must be COSMOS_FORCE_GRADIENT or COSMOS_FORCE_SPECTRAL");
+    if (cfg->force_mode != COSMOS_FORCE_GRADIENT && !is_spectral(cfg->force_mode))
+        return cpm::fail(COSMOS_ERR_INVALID, "force_mode must be one of the COSMOS_FORCE_* modes");
+    if (is_tc(cfg->force_mode) && !cpm::tc_fft_supported(N))
+        return cpm::fail(COSMOS_ERR_INVALID, "the tensor-core force modes support lattice_n 1024, 2048 and 4096");
     if (cfg->sort_granularity != -1 &&
         (cfg->sort_granularity < 4 || cfg->sort_granularity > 6 || (N >> cfg->sort_granularity) < 1))
         return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity must be -1 (default) or 4..6 with 2^g <= N");
@@ -465,10 +484,20 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         cudaMemsetAsync(h->force, 0, NN * sizeof(float2), h->stream) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "initialisation"));
     if (cpm::prepare_conv_passes(N) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "kernel attributes"));
-    if (cfg->force_mode == COSMOS_FORCE_SPECTRAL) {
+    if (is_spectral(cfg->force_mode)) {
         if ((rc = dalloc(&h->spec2, NN / 2)) || (rc = dalloc(&h->edge, size_t(N / 2) * 4)) ||
             (rc = dalloc(&h->dy, size_t(3) * N)))
             return bail(rc);
+        if (is_tc(cfg->force_mode)) {
+            const int bf16 = cfg->force_mode == COSMOS_FORCE_SPECTRAL_TC_BF16;
+            if ((rc = dalloc(reinterpret_cast<unsigned char**>(&h->tc_dft), cpm::tc_dft_bytes(N))) ||
+                (rc = dalloc(&h->tc_status, 1)))
+                return bail(rc);
+            if (cudaMemsetAsync(h->tc_status, 0, sizeof(int), h->stream) != cudaSuccess ||
+                cpm::prepare_tc_columns(N, bf16, h->tc_dft, h->stream) != cudaSuccess)
+                return bail(cpm::fail(COSMOS_ERR_CUDA, "tensor-core column pass setup"));
+            h->tc = cpm::SpectralTc{bf16, h->tc_dft, h->tc_status};
+        }
         if (cpm::prepare_spectral_passes(N) != cudaSuccess)
             return bail(cpm::fail(COSMOS_ERR_CUDA, "spectral kernel attributes"));
         if (cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -759,6 +788,14 @@ int cosmos_pm_synchronize(cosmos_pm* h) {
     auto impl = [&]() -> int {
         CPM_CUDA(cudaStreamSynchronize(h->stream));
         CPM_CUDA(cudaStreamSynchronize(h->copy_stream));
+        if (h->tc_status) {  // a tensor-core completion wait that gave up
+            int st = 0;
+            CPM_CUDA(cudaMemcpy(&st, h->tc_status, sizeof(int), cudaMemcpyDeviceToHost));
+            if (st) {
+                CPM_CUDA(cudaMemset(h->tc_status, 0, sizeof(int)));
+                return cpm::fail(COSMOS_ERR_TIMEOUT, "tensor-core column pass: an MMA completion wait timed out");
+            }
+        }
         return COSMOS_OK;
     };
     return finish(h, impl());
@@ -811,11 +848,9 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
                 CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
                 break;
             case COSMOS_STAGE_FORCE:
-                // gradient mode: from the potential field; spectral mode: from the density
-                if (h->cfg.force_mode == COSMOS_FORCE_SPECTRAL)
-                    CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq,
-                                                        h->force, h->tw, h->cfg.gravity_multiplier, st,
-                                                        h->aux_stream, h->fork_ev, h->join_ev));
+                // gradient mode: from the potential field; spectral modes: from the density
+                if (is_spectral(h->cfg.force_mode))
+                    CPM_TRY(launch_spectral(h, st));
                 else
                     CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, h->cfg.gravity_multiplier, st));
                 break;
@@ -968,7 +1003,7 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream) {
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
     if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
     // force passes + fused step kernel (the density clear is a memset node)
-    const int force = h->cfg.force_mode == COSMOS_FORCE_SPECTRAL ? cpm::spectral_launches_per_step()
+    const int force = is_spectral(h->cfg.force_mode) ? cpm::spectral_launches_per_step()
                                                                  : cpm::conv_launches_per_step() + 1;
     *launches = force + 1;
     return COSMOS_OK;

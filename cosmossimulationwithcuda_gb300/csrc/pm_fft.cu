@@ -545,14 +545,21 @@ struct SpecShape {
 template <int N>
 static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                      const float* kq, float2* force, const float2* tw, float g, int batch,
-                                     cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join) {
+                                     cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join,
+                                     const SpectralTc* tc) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
     cudaError_t e;
     k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
-    k_cols_spectral<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, SS::col_smem, st>>>(spec, spec2, edge,
-                                                                                                    kq, tw, g);
+    if (tc) {
+        if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status, batch,
+                                         st)) != cudaSuccess)
+            return e;
+    } else {
+        k_cols_spectral<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, SS::col_smem, st>>>(
+            spec, spec2, edge, kq, tw, g);
+    }
     if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
     k_rows_c2r<N, 1, SS::ENT, 4><<<dim3(3, batch), SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
@@ -588,12 +595,14 @@ cudaError_t prepare_spectral_passes(int N) {
 
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch) {
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch,
+                                  const SpectralTc* tc) {
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
+    if (tc && !tc_fft_supported(N)) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join);
+        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join, tc);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:

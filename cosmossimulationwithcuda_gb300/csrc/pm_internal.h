@@ -17,10 +17,24 @@ int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st)
 // reference's clamped-edge stencil applied in Fourier space.  spec2: N*N/2
 // float2; edge: (N/2)*4 float2; dy: 3*N float.
 cudaError_t prepare_spectral_passes(int N);
-// aux/fork/join: an auxiliary stream and two events for the concurrent edge pass.
+// Tensor-core column pass (pm_fft_tc.cu): split-precision DFT stages.
+struct SpectralTc {
+    int bf16;         // 1: BF16 split, 0: FP16 split
+    const void* dft;  // DFT matrix image (tc_dft_bytes(N) bytes, prepare_tc_columns)
+    int* status;      // set to 1 when an MMA completion wait timed out
+};
+bool tc_fft_supported(int N);
+size_t tc_dft_bytes(int N);
+cudaError_t prepare_tc_columns(int N, int bf16, void* dft_dev, cudaStream_t st);
+cudaError_t launch_cols_spectral_tc(int N, int bf16, float2* spec, float2* spec2, float2* edge, const float* kq,
+                                    const float2* tw, const void* dft_dev, float g, int* status, int batch,
+                                    cudaStream_t st);
+// aux/fork/join: an auxiliary stream and two events for the concurrent edge pass;
+// tc: the tensor-core column pass instead of the FP32 one (nullptr: FP32).
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1);
+                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1,
+                                  const SpectralTc* tc = nullptr);
 int spectral_launches_per_step();
 
 // pm_particles.cu

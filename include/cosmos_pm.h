@@ -59,6 +59,13 @@ extern "C" {
  *            against FP64 at the same memory traffic). */
 #define COSMOS_FORCE_GRADIENT 0
 #define COSMOS_FORCE_SPECTRAL 1
+/* SPECTRAL with the column FFTs (3 of the step's 5 length-N transforms) on
+ * the tensor cores: each transform is a four-step FFT whose two DFT stages
+ * are tcgen05 GEMMs on split 16-bit operands (high part + rounding of the
+ * remainder, three products accumulated in FP32).  FP16 split (range-scaled)
+ * or BF16 split.  N = 1024, 2048 or 4096 only. */
+#define COSMOS_FORCE_SPECTRAL_TC_FP16 2
+#define COSMOS_FORCE_SPECTRAL_TC_BF16 3
 
 typedef struct cosmos_pm_config {
     int32_t lattice_n;          /* N: power of two, 16..8192   (Constants::N, CosmosCuda.cuh:38) */
