@@ -208,17 +208,23 @@ def _cic_sample(F, x, y, N):
             + Ff[c + N] * ((1 - fx) * fy)[:, None] + Ff[c + N + 1] * (fx * fy)[:, None])
 
 
+_FP64_FORCE = {}
+
+
 def force_error_vs_fp64(state, N, cic, dt, F_gpu):
     """Relative L2 error of the GPU force against the FP64 oracle on the same
     positions: over the lattice, and sampled at the particles."""
     from oracle import pm_oracle
-    pm_oracle.set_threads(os.cpu_count() or 1)
-    o = pm_oracle.OraclePM(N, cic, dt, 1.0, fp64=True)
-    o.deposit(state.x, state.y, state.m)
-    o.potential()
-    o.gradient()
-    ref = o.force()
-    o.close()
+    key = (id(state), N, cic)
+    ref = _FP64_FORCE.get(key)
+    if ref is None:
+        pm_oracle.set_threads(os.cpu_count() or 1)
+        o = pm_oracle.OraclePM(N, cic, dt, 1.0, fp64=True)
+        o.deposit(state.x, state.y, state.m)
+        o.potential()
+        o.gradient()
+        ref = _FP64_FORCE[key] = o.force()
+        o.close()
     lattice = float(np.linalg.norm(F_gpu - ref) / np.linalg.norm(ref))
     a = _cic_sample(F_gpu, state.x, state.y, N)
     b = _cic_sample(ref, state.x, state.y, N)
@@ -344,6 +350,8 @@ def main():
                     help="e2e: read the positions back every this many steps")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the sort granularity / cadence with cosmos_pm_autotune on this state first")
+    ap.add_argument("--no-tc-compare", action="store_true",
+                    help="skip the tensor-core split-FFT comparison run of the headline metric")
     ap.add_argument("--workload", default=WORKLOAD,
                     help="the headline disk (default), another single-simulation workload "
                          "(uniform-1M-512-ngp, collide-100M-4096-cic, clumpy-1B-8192-cic) or "
@@ -528,6 +536,34 @@ def main():
     launches = sim.launches_per_step() * args.steps
     sim.close()
 
+    # ---- the metric's second arm: the same step with the tensor-core split FFT ----
+    tc_arm = None
+    if rank == 0 and not args.no_tc_compare and mode == _lib.FORCE_SPECTRAL and N in (1024, 2048, 4096):
+        try:
+            tsteps = min(args.steps, 300)
+            with _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=sort_interval,
+                                 sort_granularity=sort_gran, force_mode=_lib.FORCE_SPECTRAL_TC_FP16) as ts:
+                ts.set_state(state)
+                terr = None
+                if not args.no_force_check:
+                    ts.run_stage(_lib.STAGE_DEPOSIT)
+                    ts.run_stage(_lib.STAGE_FORCE)
+                    terr = force_error_vs_fp64(state, N, cic, dt, ts.get_field(_lib.FIELD_FORCE))
+                    ts.set_state(state)
+                ts.step(args.warmup)
+                ts.synchronize()
+                a, b = rt.event(), rt.event()
+                rt.record(a, ts.stream())
+                ts.step(tsteps)
+                rt.record(b, ts.stream())
+                tms = rt.elapsed_ms(a, b) / tsteps
+                ts.synchronize()
+            tc_arm = {"value": P / (tms / 1e3), "unit": UNIT, "ms_per_step": tms, "steps": tsteps,
+                      "force_rel_err_vs_fp64": terr, "precision": "FP16 hi/lo split operands, FP32 accumulate",
+                      "note": "column FFTs (3 of the 5 length-N transforms per step) as tcgen05 GEMMs"}
+        except Exception as exc:
+            tc_arm = {"unavailable": str(exc)}
+
     # ---- the reference's own step on the same GPU (its kernels + cuFFT) ----
     ref_gpu = None
     if rank == 0 and not args.no_reference_gpu:
@@ -555,7 +591,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches, "stages_ms": stages, "reference_gpu": ref_gpu,
-            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift}
+            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift, "tc_split_fft": tc_arm}
     print(json.dumps(line), flush=True)
 
 

@@ -69,6 +69,14 @@ struct ColShape {
     static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);
 };
 
+// Register budgets (resident CTAs per SM) of the spectral passes.
+#ifndef CPM_COLS_SPECTRAL_MINB
+#define CPM_COLS_SPECTRAL_MINB 3
+#endif
+#ifndef CPM_C2R_SPECTRAL_MINB
+#define CPM_C2R_SPECTRAL_MINB 2
+#endif
+
 // Minimum resident CTAs per SM for a block size (register budget of launch bounds).
 template <int NT>
 struct MinBlocks {
@@ -293,7 +301,7 @@ __device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
 // (into spec2); and the three y-edge differences of every line,
 // edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, 3) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
+__global__ void __launch_bounds__(NT, CPM_COLS_SPECTRAL_MINB) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
                                                          float2* __restrict__ edge, const float* __restrict__ kq,
                                                          const float2* __restrict__ tw, float g) {
     using C = float2;
@@ -366,7 +374,7 @@ __global__ void __launch_bounds__(NT, 3) k_cols_spectral(float2* __restrict__ sp
 // with the x-edge corrections from Phi, written as interleaved (fx, fy).  The
 // y-edge corrections of rows 0, 1, N-2, N-1 follow in k_apply_edge_rows.
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, 2) k_rows_c2r_spectral(const float2* __restrict__ spec,
+__global__ void __launch_bounds__(NT, CPM_C2R_SPECTRAL_MINB) k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
                                                              float4* __restrict__ force,
                                                              const float2* __restrict__ tw, float g) {

@@ -39,6 +39,12 @@ namespace cpm {
 namespace {
 
 constexpr int kFusedThreads = 256;
+// Optional register budget: resident CTAs per SM the fused kernel must allow.
+#ifdef CPM_FUSED_MIN_BLOCKS
+#define CPM_FUSED_BOUNDS __launch_bounds__(kFusedThreads, CPM_FUSED_MIN_BLOCKS)
+#else
+#define CPM_FUSED_BOUNDS __launch_bounds__(kFusedThreads)
+#endif
 
 __host__ __device__ constexpr int win_y(int gran) { return (1 << gran) + 2 * kTileHalo + 1; }
 __host__ __device__ constexpr int win_x(int gran) { return (win_y(gran) + 3) & ~3; }
@@ -265,7 +271,7 @@ __global__ void __launch_bounds__(256) k_item_scales(const float* __restrict__ m
 
 // ---- the fused step kernel, tile windows ----------------------------------------------------
 template <int CIC, int GRAN>
-__global__ void __launch_bounds__(kFusedThreads) k_fused_tiles(const WorkItem* __restrict__ items,
+__global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ items,
                                                                const uint32_t* __restrict__ n_items_p,
                                                                ParticleArrays p, const float2* __restrict__ force,
                                                                float* __restrict__ rho, int N, float dt) {
