@@ -30,7 +30,7 @@ EXPORTS = (
     "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
     "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
-    "cosmos_pm_host_alloc", "cosmos_pm_host_free", "cosmos_pm_autotune",
+    "cosmos_pm_host_alloc", "cosmos_pm_host_free", "cosmos_pm_autotune", "cosmos_pm_generate",
     "cosmos_ensemble_default_config", "cosmos_ensemble_create", "cosmos_ensemble_destroy",
     "cosmos_ensemble_set_particles", "cosmos_ensemble_get_particles", "cosmos_ensemble_step",
     "cosmos_ensemble_synchronize", "cosmos_ensemble_get_field", "cosmos_ensemble_launches_per_step",
@@ -53,6 +53,31 @@ class Config(ctypes.Structure):
         ("use_graph", ctypes.c_int32),
         ("blur_r", ctypes.c_int32),
         ("reserved", ctypes.c_int32 * 6),
+    ]
+
+
+IC_UNIFORM, IC_EXP_DISK, IC_PLUMMER, IC_RING_DISK = 0, 1, 2, 3
+
+
+class IcParams(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("black_hole", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+        ("center_x", ctypes.c_float),
+        ("center_y", ctypes.c_float),
+        ("scale", ctypes.c_float),
+        ("rmax", ctypes.c_float),
+        ("mass", ctypes.c_float),
+        ("mass_sigma", ctypes.c_float),
+        ("bulk_vx", ctypes.c_float),
+        ("bulk_vy", ctypes.c_float),
+        ("spin", ctypes.c_float),
+        ("dispersion", ctypes.c_float),
+        ("g", ctypes.c_float),
+        ("pad", ctypes.c_int32),
+        ("total_particles", ctypes.c_int64),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 
@@ -122,6 +147,7 @@ def load(path: str | None = None):
         "cosmos_pm_get_frame_async": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(ctypes.c_uint64)]),
         "cosmos_pm_host_alloc": (ctypes.c_int, [i64, ctypes.POINTER(_vp)]),
         "cosmos_pm_host_free": (ctypes.c_int, [_vp]),
+        "cosmos_pm_generate": (ctypes.c_int, [_vp, ctypes.POINTER(IcParams), i64, i64]),
         "cosmos_pm_autotune": (ctypes.c_int, [ctypes.POINTER(Config), _f32p, _f32p, _f32p, _f32p, _f32p, i32,
                                               ctypes.c_char_p, ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_float)]),
         "cosmos_ensemble_default_config": (None, [ctypes.POINTER(EnsembleConfig)]),
@@ -238,6 +264,14 @@ class Simulation:
 
     def clear(self):
         self._check(self.L.cosmos_pm_clear(self.h))
+
+    def generate(self, kind: int, count: int, offset: int = 0, **params):
+        """Seeded initial conditions on the device (cosmos_pm_generate); params
+        are the fields of cosmos_ic_params (seed, center_x, scale, ...)."""
+        ic = IcParams(kind=kind, g=1.0)
+        for k, v in params.items():
+            setattr(ic, k, int(v) if k in ("black_hole", "seed", "total_particles") else v)
+        self._check(self.L.cosmos_pm_generate(self.h, ctypes.byref(ic), count, offset))
 
     # -- stepping -------------------------------------------------------------
     def step(self, n: int = 1):

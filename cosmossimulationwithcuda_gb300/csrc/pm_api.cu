@@ -543,6 +543,46 @@ int set_particles_impl(cosmos_pm* h, const float* x, const float* y, const float
     return COSMOS_OK;
 }
 
+int generate_impl(cosmos_pm* h, const cosmos_ic_params* ic, int64_t count, int64_t offset) {
+    if (!ic) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    CPM_TRY(check_range(h, count, offset));
+    if (ic->kind < COSMOS_IC_UNIFORM || ic->kind > COSMOS_IC_RING_DISK)
+        return cpm::fail(COSMOS_ERR_INVALID, "unknown initial-condition kind");
+    if (ic->kind == COSMOS_IC_RING_DISK && ic->total_particles <= 0)
+        return cpm::fail(COSMOS_ERR_INVALID, "RING_DISK needs total_particles > 0");
+    if (ic->kind != COSMOS_IC_UNIFORM && !(ic->scale > 0.0f))
+        return cpm::fail(COSMOS_ERR_INVALID, "scale must be positive");
+    if (count == 0) return COSMOS_OK;
+    cudaStream_t st = h->stream;
+    float* tmp = nullptr;
+    if (cudaMallocAsync(&tmp, size_t(count) * 5 * sizeof(float), st) != cudaSuccess) {
+        cudaGetLastError();
+        return cpm::fail(COSMOS_ERR_NOMEM, "generation buffer");
+    }
+    float* g[5] = {tmp, tmp + count, tmp + 2 * count, tmp + 3 * count, tmp + 4 * count};
+    int rc = COSMOS_OK;
+    auto body = [&]() -> int {
+        CPM_CUDA(cpm::launch_generate(*ic, count, offset, h->N, h->cfg.dt, g[0], g[1], g[2], g[3], g[4], st));
+        ParticleArrays& p = state(h);
+        float* dsts[5] = {p.x, p.y, p.xo, p.yo, p.m};
+        if (h->identity_order) {
+            for (int i = 0; i < 5; ++i)
+                CPM_CUDA(cudaMemcpyAsync(dsts[i] + offset, g[i], size_t(count) * sizeof(float), cudaMemcpyDeviceToDevice,
+                                         st));
+        } else {
+            CPM_TRY(ensure_pos(h));
+            for (int i = 0; i < 5; ++i) CPM_CUDA(cpm::launch_scatter_by_id(g[i], h->pos, offset, count, dsts[i], st));
+        }
+        return COSMOS_OK;
+    };
+    rc = body();
+    cudaFreeAsync(tmp, st);
+    if (rc != COSMOS_OK) return rc;
+    CPM_CUDA(cudaStreamSynchronize(st));
+    state_rewritten(h);
+    return COSMOS_OK;
+}
+
 int get_particles_impl(cosmos_pm* h, float* x, float* y, float* xo, float* yo, float* m, int64_t count,
                        int64_t offset) {
     CPM_TRY(check_range(h, count, offset));
@@ -749,6 +789,12 @@ int cosmos_pm_set_particles(cosmos_pm* h, const float* x, const float* y, const 
     if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
     DeviceGuard g(h->device);
     return finish(h, set_particles_impl(h, x, y, xo, yo, m, count, offset));
+}
+
+int cosmos_pm_generate(cosmos_pm* h, const cosmos_ic_params* ic, int64_t count, int64_t offset) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, generate_impl(h, ic, count, offset));
 }
 
 int cosmos_pm_get_particles(cosmos_pm* h, float* x, float* y, float* xo, float* yo, float* m, int64_t count,

@@ -118,6 +118,10 @@ cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, c
 cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
                                 float dt, int nsm, cudaStream_t st);
 
+// pm_ics.cu -- seeded initial conditions; particle i draws from (seed, first + i)
+cudaError_t launch_generate(const cosmos_ic_params& p, int64_t count, int64_t first, int N, float dt, float* x,
+                            float* y, float* xo, float* yo, float* m, cudaStream_t st);
+
 // pm_render.cu -- display frame of the density (the reference's render chain)
 void render_weights(int R, float* w);
 cudaError_t render_init(uint32_t* state, float* extremes, cudaStream_t st);

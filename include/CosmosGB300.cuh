@@ -22,9 +22,10 @@
 // Differences, all on purpose:
 //  - one GPU per Universe: NUM_CUDA_DEVICES must be 1 (the multi-GPU lattice
 //    broadcast of the reference is not part of this library);
-//  - the random initial fill of the constructor and addGalaxy draw from a
-//    seeded std::mt19937 (seed() below) instead of std::random_device, so
-//    runs repeat; the formulas are the reference's;
+//  - the random fills of the constructor and addGalaxy run on the device
+//    (cosmos_pm_generate, counter-based and seeded: seed() below) instead of
+//    on host threads with std::random_device, so runs repeat on any machine;
+//    the formulas are the reference's;
 //  - errors print "GPUassert: <message>" and exit like the reference's
 //    gpuErrchk (CosmosCuda.cuh:19-27), or throw std::runtime_error when
 //    COSMOS_GB300_THROW is defined;
@@ -43,7 +44,6 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
-#include <random>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -100,7 +100,6 @@ struct Universe {
     static_assert(Constants::MAX_FRAMES_BUFFERED >= 2, "MAX_FRAMES_BUFFERED must be at least 2");
 
    private:
-    std::vector<float> x, y, xOld, yOld, m;
     int particleCounter = 0;
     int totalNumParticles = 0;
     cosmos_pm* sim = nullptr;
@@ -118,41 +117,13 @@ struct Universe {
 
     void check(int rc, const char* call) { cosmos_gb300_detail::check(rc, sim, call); }
 
-    // The random fills run over fixed blocks of kFillBlock particles, each with
-    // its own engine seeded from (seed, fill call, block), spread over the host
-    // threads: the result does not depend on the thread count.
-    static constexpr int kFillBlock = 1 << 16;
-
-    std::mt19937 engine(int block) const {
-        std::seed_seq s{uint32_t(rng_seed), uint32_t(rng_seed >> 32), uint32_t(rng_calls), uint32_t(block)};
-        return std::mt19937(s);
-    }
-
-    // f(block, lo, hi) for the blocks of [begin, end), on all host threads.
-    template <class F>
-    static void parallel_blocks(int begin, int end, F&& f) {
-        if (end <= begin) return;
-        const int nblocks = (end - begin + kFillBlock - 1) / kFillBlock;
-        const int hc = std::thread::hardware_concurrency() > 0 ? int(std::thread::hardware_concurrency()) : 1;
-        const int nthreads = hc < nblocks ? hc : nblocks;
-        std::vector<std::thread> ts;
-        for (int th = 0; th < nthreads; ++th)
-            ts.emplace_back([&, th]() {
-                for (int b = th; b < nblocks; b += nthreads) {
-                    const int lo = begin + b * kFillBlock;
-                    const int hi = lo + kFillBlock < end ? lo + kFillBlock : end;
-                    f(b, lo, hi);
-                }
-            });
-        for (auto& t : ts) t.join();
-    }
-
-    void upload(int start, int count) {
+    // Each random fill is one call of the device generator with its own seed
+    // (Universe seed + fill counter); particle i draws from (seed, i).
+    void generate(cosmos_ic_params ic, int count, int offset) {
         if (count <= 0) return;
+        ic.seed = rng_seed + 0x9E3779B97F4A7C15ull * (++rng_calls);
         std::lock_guard<std::mutex> g(simLock);
-        check(cosmos_pm_set_particles(sim, x.data() + start, y.data() + start, xOld.data() + start,
-                                      yOld.data() + start, m.data() + start, count, start),
-              "cosmos_pm_set_particles");
+        check(cosmos_pm_generate(sim, &ic, count, offset), "cosmos_pm_generate");
     }
 
     void pushFrame(const float* frame) {  // CosmosCuda.cuh:1302-1308
@@ -190,26 +161,14 @@ struct Universe {
         void* p = nullptr;
         check(cosmos_pm_host_alloc(int64_t(sizeof(float)) * Constants::N * Constants::N, &p), "cosmos_pm_host_alloc");
         frame_h = static_cast<float*>(p);
-        x.resize(particles);
-        y.resize(particles);
-        xOld.resize(particles);
-        yOld.resize(particles);
-        m.resize(particles);
         // uniform fill of [0.01 N, 0.99 N), at rest, equal masses 1/particles (:929-950)
-        const float mass = particles > 0 ? 1.0f / float(particles) : 0.0f;
-        parallel_blocks(0, particles, [&](int b, int lo, int hi) {
-            std::uniform_real_distribution<float> dist(0.0f, 1.0f);
-            std::mt19937 rng = engine(b);
-            for (int i = lo; i < hi; ++i) {
-                x[i] = 0.01f * Constants::N + (0.98f * dist(rng) * Constants::N);
-                y[i] = 0.01f * Constants::N + (0.98f * dist(rng) * Constants::N);
-                xOld[i] = x[i];
-                yOld[i] = y[i];
-                m[i] = mass;
-            }
-        });
-        ++rng_calls;
-        upload(0, particles);
+        cosmos_ic_params ic{};
+        ic.kind = COSMOS_IC_UNIFORM;
+        ic.center_x = ic.center_y = 0.5f * Constants::N;
+        ic.scale = 0.49f * Constants::N;
+        ic.mass = 1.0f;
+        ic.g = Constants::gravityMultiplier;
+        generate(ic, particles, 0);
         // the reference leaves the counter at the end: the next addGalaxy
         // without clear() adds nothing and wraps the counter to 0 (:967, :1171-1173)
         particleCounter = particles;
@@ -220,9 +179,6 @@ struct Universe {
 
     // Moves all particles out of the simulation area (:1037-1069).
     void clear() {
-        parallel_blocks(0, totalNumParticles, [&](int, int lo, int hi) {
-            for (int i = lo; i < hi; ++i) x[i] = y[i] = xOld[i] = yOld[i] = -10.0f;
-        });
         {
             std::lock_guard<std::mutex> g(simLock);
             check(cosmos_pm_clear(sim), "cosmos_pm_clear");
@@ -231,50 +187,28 @@ struct Universe {
     }
 
     // Adds a galaxy of n particles centred at (cx, cy) in normalised
-    // coordinates, on the reference's orbit formulas (:1071-1175).
+    // coordinates: the reference's ring-disk formulas (:1071-1175), drawn on
+    // the device (COSMOS_IC_RING_DISK).
     void addGalaxy(int n, float normalizedCenterX = 0.5f, float normalizedCenterY = 0.5f,
                    float angularVelocity = 1.0f, float massPerParticle = 1.0f, float normalizedRadius = 0.3f,
                    float centerOfMassVelocityX = 0.0f, float centerOfMassVelocityY = 0.0f, bool blackHole = false) {
         const int start = particleCounter;
         const int maxCount = (particleCounter + n < totalNumParticles) ? particleCounter + n : totalNumParticles;
         const int count = maxCount - start;
-        angularVelocity /= Constants::dt;
-        const float R = Constants::N * normalizedRadius;
-        const float radiusSquared = R * R;
-        const float totalMass = massPerParticle * count + (blackHole ? count * massPerParticle / 1000.0f : 0.0f);
-        centerOfMassVelocityX /= Constants::dt;
-        centerOfMassVelocityY /= Constants::dt;
-        const float cxN = normalizedCenterX * Constants::N, cyN = normalizedCenterY * Constants::N;
-        if (count <= 0) {  // nothing to add and no draw made; the counter still wraps at the end
-            particleCounter = maxCount >= totalNumParticles ? 0 : maxCount;
-            return;
-        }
-        parallel_blocks(start, maxCount, [&](int b, int lo, int hi) {
-            std::uniform_real_distribution<float> dist(0.0f, 1.0f);
-            std::mt19937 rng = engine(b);
-            for (int i = lo; i < hi; ++i) {
-                const float r = (0.1f + 0.9f * dist(rng)) * R;
-                const float a = float(Constants::MATH_PI * 2.0 * dist(rng));
-                const float speed = std::sqrt(0.0000044f * totalMass * r / radiusSquared);
-                x[i] = r * std::cos(a) + cxN;
-                y[i] = r * std::sin(a) + cyN;
-                const float vecX = x[i] - cxN;
-                const float vecY = y[i] - cyN;
-                xOld[i] = -Constants::dt * ((vecY * angularVelocity) * speed + centerOfMassVelocityX * Constants::N) + x[i];
-                yOld[i] = -Constants::dt * ((-vecX * angularVelocity) * speed + centerOfMassVelocityY * Constants::N) + y[i];
-                m[i] = massPerParticle / totalNumParticles;
-                if (i == maxCount - 1 && blackHole) {  // a heavy particle at the centre
-                    x[i] = cxN;
-                    y[i] = cyN;
-                    xOld[i] = x[i] - centerOfMassVelocityX * Constants::N * Constants::dt;
-                    yOld[i] = y[i] - centerOfMassVelocityY * Constants::N * Constants::dt;
-                    m[i] = (count * massPerParticle / 1000.0f) / totalNumParticles;
-                }
-            }
-        });
-        ++rng_calls;
+        cosmos_ic_params ic{};
+        ic.kind = COSMOS_IC_RING_DISK;
+        ic.black_hole = blackHole ? 1 : 0;
+        ic.center_x = normalizedCenterX;
+        ic.center_y = normalizedCenterY;
+        ic.scale = normalizedRadius;
+        ic.mass = massPerParticle;
+        ic.bulk_vx = centerOfMassVelocityX;
+        ic.bulk_vy = centerOfMassVelocityY;
+        ic.spin = angularVelocity;
+        ic.g = Constants::gravityMultiplier;
+        ic.total_particles = totalNumParticles;
+        generate(ic, count, start);
         particleCounter = maxCount;
-        upload(start, count);
         if (particleCounter >= totalNumParticles) particleCounter = 0;
     }
 

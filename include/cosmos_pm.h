@@ -154,6 +154,45 @@ int cosmos_pm_poll(cosmos_pm* h, uint64_t ticket, int32_t* done);
 /* Block until the copy behind `ticket` has landed. */
 int cosmos_pm_wait(cosmos_pm* h, uint64_t ticket);
 
+/* ---- seeded initial conditions on the device --------------------------------
+ * Replaces the host fills of the constructor (CosmosCuda.cuh:929-950) and of
+ * addGalaxy (:1071-1116), which draw from std::random_device.  Particle i of
+ * a generated set draws from a counter-based stream keyed by (seed, i), with
+ * i the particle's identity, and every float operation is a separately
+ * rounded float32 operation, so the result is reproducible bit for bit (on
+ * any GPU and by the float32 restatement in the test oracle).  Positions and
+ * velocities of identity i depend only on (seed, i) and the parameters; the
+ * per-particle mass is `mass` over the call's count. */
+#define COSMOS_IC_UNIFORM 0    /* square of half-width scale, Gaussian velocities */
+#define COSMOS_IC_EXP_DISK 1   /* exponential disk, circular speeds from the enclosed mass */
+#define COSMOS_IC_PLUMMER 2    /* projected Plummer sphere, circular speeds */
+#define COSMOS_IC_RING_DISK 3  /* the reference's addGalaxy ring disk */
+typedef struct cosmos_ic_params {
+    int32_t kind;             /* COSMOS_IC_* */
+    int32_t black_hole;       /* RING_DISK: the last particle is a heavy body at the centre */
+    uint64_t seed;
+    float center_x, center_y; /* cells; RING_DISK: fractions of N (normalizedCenterX/Y) */
+    float scale;              /* UNIFORM half-width, EXP_DISK scale length, PLUMMER radius a (cells);
+                                 RING_DISK normalizedRadius */
+    float rmax;               /* EXP_DISK / PLUMMER truncation radius (cells); <= 0: none */
+    float mass;               /* total mass of the generated particles; RING_DISK massPerParticle */
+    float mass_sigma;         /* lognormal spread of the masses (0: equal); not RING_DISK */
+    float bulk_vx, bulk_vy;   /* bulk velocity (cells per unit time);
+                                 RING_DISK centerOfMassVelocityX/Y */
+    float spin;               /* EXP_DISK / PLUMMER rotation sense (+1, -1, 0); RING_DISK angularVelocity */
+    float dispersion;         /* UNIFORM velocity sigma; EXP_DISK / PLUMMER sigma per axis as a
+                                 fraction of the circular speed */
+    float g;                  /* gravity multiplier of the circular speeds */
+    int32_t pad;
+    int64_t total_particles;  /* RING_DISK: the reference's totalNumParticles (mass divisor) */
+    int32_t reserved[4];
+} cosmos_ic_params;
+
+/* Generate `count` particles of one family into identities [offset,
+ * offset+count) on the device (synchronous).  xOld = x - v dt with the
+ * handle's dt (RING_DISK: the reference's xOld formula). */
+int cosmos_pm_generate(cosmos_pm* h, const cosmos_ic_params* ic, int64_t count, int64_t offset);
+
 /* ---- stage-level access (test hooks; the reference's private step methods) */
 #define COSMOS_FIELD_DENSITY 0   /* N*N float: accumulator_d after deposit (:1242) */
 #define COSMOS_FIELD_POTENTIAL 1 /* N*N float: latticeShifted_d (:1297) */

@@ -68,3 +68,8 @@ def test_universe_dropin_header_compiles():
 def test_ensemble_config_layout(cosmos_lib):
     import ctypes as C
     assert C.sizeof(cosmos_lib.EnsembleConfig) == 4 * 8 + 4 * 8  # matches cosmos_ensemble_config
+
+
+def test_ic_params_layout(cosmos_lib):
+    import ctypes as C
+    assert C.sizeof(cosmos_lib.IcParams) == 88  # matches cosmos_ic_params
