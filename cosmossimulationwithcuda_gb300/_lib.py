@@ -20,6 +20,7 @@ DEPOSIT_NGP, DEPOSIT_CIC = 0, 1
 FORCE_GRADIENT, FORCE_SPECTRAL, FORCE_SPECTRAL_TC_FP16, FORCE_SPECTRAL_TC_BF16 = 0, 1, 2, 3
 FIELD_DENSITY, FIELD_POTENTIAL, FIELD_FORCE = 0, 1, 2
 STAGE_DEPOSIT, STAGE_POTENTIAL, STAGE_FORCE, STAGE_INTEGRATE = 0, 1, 2, 3
+TEST_FAIL_ALLOC, TEST_TC_SKIP_MMA = 1, 2
 
 # Every function include/cosmos_pm.h declares (checked by the CPU test suite).
 EXPORTS = (
@@ -31,6 +32,7 @@ EXPORTS = (
     "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
     "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
     "cosmos_pm_host_alloc", "cosmos_pm_host_free", "cosmos_pm_autotune", "cosmos_pm_generate",
+    "cosmos_pm_checkpoint_save", "cosmos_pm_checkpoint_load", "cosmos_pm_steps_taken", "cosmos_pm_test_hook",
     "cosmos_ensemble_default_config", "cosmos_ensemble_create", "cosmos_ensemble_destroy",
     "cosmos_ensemble_set_particles", "cosmos_ensemble_get_particles", "cosmos_ensemble_step",
     "cosmos_ensemble_synchronize", "cosmos_ensemble_get_field", "cosmos_ensemble_launches_per_step",
@@ -148,6 +150,10 @@ def load(path: str | None = None):
         "cosmos_pm_host_alloc": (ctypes.c_int, [i64, ctypes.POINTER(_vp)]),
         "cosmos_pm_host_free": (ctypes.c_int, [_vp]),
         "cosmos_pm_generate": (ctypes.c_int, [_vp, ctypes.POINTER(IcParams), i64, i64]),
+        "cosmos_pm_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+        "cosmos_pm_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+        "cosmos_pm_steps_taken": (ctypes.c_int, [_vp, ctypes.POINTER(i64)]),
+        "cosmos_pm_test_hook": (ctypes.c_int, [_vp, i32, i64]),
         "cosmos_pm_autotune": (ctypes.c_int, [ctypes.POINTER(Config), _f32p, _f32p, _f32p, _f32p, _f32p, i32,
                                               ctypes.c_char_p, ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_float)]),
         "cosmos_ensemble_default_config": (None, [ctypes.POINTER(EnsembleConfig)]),
@@ -264,6 +270,20 @@ class Simulation:
 
     def clear(self):
         self._check(self.L.cosmos_pm_clear(self.h))
+
+    def save(self, path: str):
+        self._check(self.L.cosmos_pm_checkpoint_save(self.h, path.encode()))
+
+    def load(self, path: str):
+        self._check(self.L.cosmos_pm_checkpoint_load(self.h, path.encode()))
+
+    def steps_taken(self) -> int:
+        n = ctypes.c_int64()
+        self._check(self.L.cosmos_pm_steps_taken(self.h, ctypes.byref(n)))
+        return n.value
+
+    def test_hook(self, hook: int, value: int):
+        self._check(self.L.cosmos_pm_test_hook(self.h, hook, value))
 
     def generate(self, kind: int, count: int, offset: int = 0, **params):
         """Seeded initial conditions on the device (cosmos_pm_generate); params
@@ -446,3 +466,10 @@ class Ensemble:
         s = ctypes.c_uint64()
         self._check(self.L.cosmos_ensemble_stream(self.h, ctypes.byref(s)))
         return s.value
+
+
+def test_hook(hook: int, value: int):
+    """Library-wide test hook (cosmos_pm_test_hook with no handle)."""
+    rc = load().cosmos_pm_test_hook(None, hook, value)
+    if rc != COSMOS_OK:
+        raise CosmosError(rc, load().cosmos_pm_last_error(None).decode())

@@ -7,7 +7,9 @@
 // :1318-1364, destructor :1396-1427) and its render chain (:1249-1256, kernels
 // in pm_render.cu).  The frame ring and worker thread live in the C++ drop-in
 // header (include/CosmosGB300.cuh); the multi-GPU exchange is not built.
+#include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -27,6 +29,17 @@ int fail(int code, const std::string& msg) {
 }
 
 const char* last_error_message() { return g_last_error.c_str(); }
+
+// COSMOS_TEST_FAIL_ALLOC: allocations left before the one that fails (0: off).
+static std::atomic<int64_t> g_fail_alloc_countdown{0};
+
+bool alloc_should_fail() {
+    int64_t c = g_fail_alloc_countdown.load();
+    while (c > 0) {
+        if (g_fail_alloc_countdown.compare_exchange_weak(c, c - 1)) return c == 1;
+    }
+    return false;
+}
 
 }  // namespace cpm
 
@@ -107,6 +120,7 @@ struct cosmos_pm {
 
     bool use_graph = true;
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer parity][tiled]
+    int64_t steps_taken = 0;  // steps advanced since creation (restored by a checkpoint load)
 
     std::string err;
 };
@@ -133,6 +147,11 @@ int finish(cosmos_pm* h, int rc) {
 template <class T>
 int dalloc(T** p, size_t n) {
     if (n == 0) n = 1;
+    if (cpm::alloc_should_fail()) {
+        *p = nullptr;
+        return cpm::fail(COSMOS_ERR_NOMEM, "device allocation of " + std::to_string(n * sizeof(T)) +
+                                               " bytes failed (injected by COSMOS_TEST_FAIL_ALLOC)");
+    }
     if (cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T)) != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;
@@ -263,6 +282,7 @@ int enqueue_step(cosmos_pm* h) {
         CPM_TRY(enqueue_step_body(h, h->stream, false));
     }
     ++h->steps_since_sort;
+    ++h->steps_taken;
     return COSMOS_OK;
 }
 
@@ -540,6 +560,79 @@ int set_particles_impl(cosmos_pm* h, const float* x, const float* y, const float
     }
     CPM_CUDA(cudaStreamSynchronize(st));
     state_rewritten(h);
+    return COSMOS_OK;
+}
+
+int get_particles_impl(cosmos_pm* h, float* x, float* y, float* xo, float* yo, float* m, int64_t count,
+                       int64_t offset);
+
+// ---- checkpoints: header + the five particle arrays in identity order ----
+struct CheckpointHeader {
+    char magic[8];  // "COSMOSPM"
+    uint32_t version;
+    int32_t lattice_n, deposit, force_mode;
+    int64_t num_particles;
+    float dt, gravity_multiplier;
+    int64_t steps;
+    uint64_t checksum;  // FNV-1a over the array bytes
+};
+constexpr uint32_t kCheckpointVersion = 1;
+
+uint64_t fnv1a(uint64_t h, const void* data, size_t n) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 0x100000001B3ull;
+    return h;
+}
+
+int checkpoint_save_impl(cosmos_pm* h, const char* path) {
+    if (!path) return cpm::fail(COSMOS_ERR_INVALID, "null path");
+    const size_t P = size_t(h->P);
+    std::vector<float> a(P * 5);
+    CPM_TRY(get_particles_impl(h, a.data(), a.data() + P, a.data() + 2 * P, a.data() + 3 * P, a.data() + 4 * P,
+                               h->P, 0));
+    CheckpointHeader hd{};
+    std::memcpy(hd.magic, "COSMOSPM", 8);
+    hd.version = kCheckpointVersion;
+    hd.lattice_n = h->N;
+    hd.deposit = h->cfg.deposit;
+    hd.force_mode = h->cfg.force_mode;
+    hd.num_particles = h->P;
+    hd.dt = h->cfg.dt;
+    hd.gravity_multiplier = h->cfg.gravity_multiplier;
+    hd.steps = h->steps_taken;
+    hd.checksum = fnv1a(0xCBF29CE484222325ull, a.data(), a.size() * sizeof(float));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return cpm::fail(COSMOS_ERR_INVALID, std::string("cannot open ") + path + " for writing");
+    const bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
+                    std::fwrite(a.data(), sizeof(float), a.size(), f) == a.size();
+    const bool closed = std::fclose(f) == 0;
+    if (!ok || !closed) return cpm::fail(COSMOS_ERR_INVALID, std::string("writing ") + path + " failed");
+    return COSMOS_OK;
+}
+
+int checkpoint_load_impl(cosmos_pm* h, const char* path) {
+    if (!path) return cpm::fail(COSMOS_ERR_INVALID, "null path");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return cpm::fail(COSMOS_ERR_INVALID, std::string("cannot open ") + path);
+    CheckpointHeader hd{};
+    const size_t P = size_t(h->P);
+    std::vector<float> a(P * 5);
+    const bool got_header = std::fread(&hd, sizeof(hd), 1, f) == 1;
+    const bool got_data = got_header && std::fread(a.data(), sizeof(float), a.size(), f) == a.size();
+    const bool at_end = got_data && std::fgetc(f) == EOF;
+    std::fclose(f);
+    if (!got_header || std::memcmp(hd.magic, "COSMOSPM", 8) != 0 || hd.version != kCheckpointVersion)
+        return cpm::fail(COSMOS_ERR_INVALID, std::string(path) + " is not a cosmos_pm checkpoint");
+    if (hd.lattice_n != h->N || hd.num_particles != h->P || hd.deposit != h->cfg.deposit ||
+        hd.dt != h->cfg.dt || hd.gravity_multiplier != h->cfg.gravity_multiplier)
+        return cpm::fail(COSMOS_ERR_INVALID, "checkpoint made with a different lattice, particle count, deposit, "
+                                             "time step or gravity multiplier");
+    if (!got_data || !at_end) return cpm::fail(COSMOS_ERR_INVALID, std::string(path) + " is truncated or too long");
+    if (fnv1a(0xCBF29CE484222325ull, a.data(), a.size() * sizeof(float)) != hd.checksum)
+        return cpm::fail(COSMOS_ERR_INVALID, std::string(path) + ": checksum mismatch");
+    CPM_TRY(set_particles_impl(h, a.data(), a.data() + P, a.data() + 2 * P, a.data() + 3 * P, a.data() + 4 * P,
+                               h->P, 0));
+    h->steps_taken = hd.steps;
     return COSMOS_OK;
 }
 
@@ -903,6 +996,7 @@ int cosmos_pm_run_stage(cosmos_pm* h, int32_t stage_id) {
             case COSMOS_STAGE_INTEGRATE:
                 CPM_CUDA(cpm::launch_integrate(h->force, p, h->P, h->N, h->cic, h->cfg.dt, h->nsm, st));
                 h->density_valid = false;  // positions moved; the density is stale
+                ++h->steps_taken;
                 break;
             default:
                 return cpm::fail(COSMOS_ERR_INVALID, "unknown stage");
@@ -1053,6 +1147,48 @@ int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
                                                                  : cpm::conv_launches_per_step() + 1;
     *launches = force + 1;
     return COSMOS_OK;
+}
+
+int cosmos_pm_checkpoint_save(cosmos_pm* h, const char* path) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, checkpoint_save_impl(h, path));
+}
+
+int cosmos_pm_checkpoint_load(cosmos_pm* h, const char* path) {
+    if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    DeviceGuard g(h->device);
+    return finish(h, checkpoint_load_impl(h, path));
+}
+
+int cosmos_pm_steps_taken(cosmos_pm* h, int64_t* steps) {
+    if (!h || !steps) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    *steps = h->steps_taken;
+    return COSMOS_OK;
+}
+
+int cosmos_pm_test_hook(cosmos_pm* h, int32_t hook, int64_t value) {
+    switch (hook) {
+        case COSMOS_TEST_FAIL_ALLOC:
+            cpm::g_fail_alloc_countdown.store(value > 0 ? value : 0);
+            return COSMOS_OK;
+        case COSMOS_TEST_TC_SKIP_MMA: {
+            if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+            if (!is_tc(h->cfg.force_mode)) return finish(h, cpm::fail(COSMOS_ERR_STATE, "not a tensor-core force mode"));
+            DeviceGuard g(h->device);
+            cudaStreamSynchronize(h->stream);
+            h->tc.skip_mma = value != 0;
+            for (auto& row : h->graph)  // captured steps hold the old kernel argument
+                for (auto& gr : row)
+                    if (gr) {
+                        cudaGraphExecDestroy(gr);
+                        gr = nullptr;
+                    }
+            return COSMOS_OK;
+        }
+        default:
+            return cpm::fail(COSMOS_ERR_INVALID, "unknown test hook");
+    }
 }
 
 int cosmos_pm_host_alloc(int64_t bytes, void** out) {

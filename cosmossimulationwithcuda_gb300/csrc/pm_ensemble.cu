@@ -96,6 +96,10 @@ int finish(cosmos_ensemble* e, int rc) {
 template <class T>
 int dalloc(T** p, size_t n) {
     if (n == 0) n = 1;
+    if (cpm::alloc_should_fail()) {
+        *p = nullptr;
+        return cpm::fail(COSMOS_ERR_NOMEM, "device allocation failed (injected by COSMOS_TEST_FAIL_ALLOC)");
+    }
     if (cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T)) != cudaSuccess) {
         cudaGetLastError();
         *p = nullptr;

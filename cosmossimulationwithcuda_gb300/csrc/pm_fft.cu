@@ -562,8 +562,8 @@ static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spe
     cudaError_t e;
     k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
     if (tc) {
-        if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status, batch,
-                                         st)) != cudaSuccess)
+        if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status,
+                                         tc->skip_mma, batch, st)) != cudaSuccess)
             return e;
     } else {
         k_cols_spectral<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, SS::col_smem, st>>>(

@@ -22,8 +22,8 @@
 // Shapes: L = 1024 (32 x 32, 4 lines per CTA), 2048 (64 x 32, 4 lines),
 // 4096 (64 x 64, 2 lines).  One CTA holds the DFT matrices, its lines (FP32)
 // and one operand buffer: 80 / 208 / 192 KB of shared memory, 128 tensor-memory
-// columns.  Waits on the MMA completion barrier are bounded; a timeout sets
-// *status and the CTA skips its remaining MMAs.
+// columns.  Waits on the MMA completion barrier are bounded (200 ms of wall
+// time); a timeout sets *status and the CTA skips its remaining MMAs.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -73,7 +73,7 @@ __device__ __forceinline__ float warp_max(float v) {
 // out(b, k, v) receives output k (to be conjugated by the caller for an inverse).
 template <int L, int BF16, class In, class Out>
 __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint32_t& phase, int* fail,
-                       float* red, const float2* __restrict__ tw, In in, Out out, int* status) {
+                       float* red, const float2* __restrict__ tw, In in, Out out, int* status, int skip_mma) {
     using S = TcShape<L>;
     constexpr int L1 = S::L1, L2 = S::L2, B = S::B;
     uint16_t* ophi = reinterpret_cast<uint16_t*>(smem + S::OFF_OPHI);
@@ -124,7 +124,7 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid == 0 && !*fail) {
+    if (tid == 0 && !*fail && !skip_mma) {
         const uint32_t idesc = tc::idesc_f16(BF16, 128, S::KA);
         const uint32_t a_hi = tc::smem_u32(ophi), a_lo = tc::smem_u32(oplo);
         const uint32_t b_hi = tc::smem_u32(f1), b_lo = tc::smem_u32(f1 + S::KA * S::KA * 2);
@@ -180,7 +180,7 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (tid == 0 && !*fail) {
+    if (tid == 0 && !*fail && !skip_mma) {
         const uint32_t idesc = tc::idesc_f16(BF16, 128, S::KC);
         const uint32_t b_hi = tc::smem_u32(f2), b_lo = tc::smem_u32(f2 + S::KC * S::KC * 2);
         for (int g = 0; g < S::GC; ++g) {
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
                                                                      const float* __restrict__ kq,
                                                                      const float2* __restrict__ tw,
                                                                      const uint4* __restrict__ fimg, float g,
-                                                                     int* __restrict__ status) {
+                                                                     int* __restrict__ status, int skip_mma) {
     using S = TcShape<L>;
     constexpr int B = S::B, M = L / 2;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
     // forward FFT over y, in place
     tc_fft<L, BF16>(
         smem, tmem, &mbar, phase, &fail, red, tw, [d0](int b, int i) { return d0[b * L + i]; },
-        [d0](int b, int k, float2 v) { d0[b * L + k] = v; }, status);
+        [d0](int b, int k, float2 v) { d0[b * L + k] = v; }, status, skip_mma);
 
     // x K (line kx = 0 packs the real spectra of kx = 0 and kx = N/2)
     for (int idx = tid; idx < B * (M + 1); idx += kTcThreads) {
@@ -373,11 +373,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
             const float S = g * (tw[(2 * i) & (L - 1)].y - 8.0f * tw[i].y) * (1.0f / 6.0f);
             return make_float2(-S * v.y, -S * v.x);  // conj(i S v)
         },
-        [out2](int b, int k, float2 v) { out2[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status);
+        [out2](int b, int k, float2 v) { out2[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status, skip_mma);
     float2* out1 = spec + size_t(kx0) * L;
     tc_fft<L, BF16>(
         smem, tmem, &mbar, phase, &fail, red, tw, [d0](int b, int i) { return cconj(d0[b * L + i]); },
-        [out1](int b, int k, float2 v) { out1[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status);
+        [out1](int b, int k, float2 v) { out1[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status, skip_mma);
 
     if (warp == 0) tc::tmem_dealloc(tmem, S::TCOLS);
 }
@@ -414,18 +414,18 @@ cudaError_t prepare_tc_columns(int N, int bf16, void* dft_dev, cudaStream_t st) 
 }
 
 cudaError_t launch_cols_spectral_tc(int N, int bf16, float2* spec, float2* spec2, float2* edge, const float* kq,
-                                    const float2* tw, const void* dft_dev, float g, int* status, int batch,
-                                    cudaStream_t st) {
+                                    const float2* tw, const void* dft_dev, float g, int* status, int skip_mma,
+                                    int batch, cudaStream_t st) {
 #define CPM_TC(n)                                                                                                 \
     if (N == n) {                                                                                                 \
         using S = TcShape<n>;                                                                                     \
         const dim3 grid((n / 2) / S::B, batch);                                                                   \
         if (bf16)                                                                                                 \
             k_cols_spectral_tc<n, 1><<<grid, kTcThreads, S::SMEM, st>>>(spec, spec2, edge, kq, tw,                \
-                                                                        static_cast<const uint4*>(dft_dev), g, status); \
+                                                                        static_cast<const uint4*>(dft_dev), g, status, skip_mma); \
         else                                                                                                      \
             k_cols_spectral_tc<n, 0><<<grid, kTcThreads, S::SMEM, st>>>(spec, spec2, edge, kq, tw,                \
-                                                                        static_cast<const uint4*>(dft_dev), g, status); \
+                                                                        static_cast<const uint4*>(dft_dev), g, status, skip_mma); \
         return cudaGetLastError();                                                                                \
     }
     CPM_TC(1024) CPM_TC(2048) CPM_TC(4096)

@@ -22,13 +22,16 @@ struct SpectralTc {
     int bf16;         // 1: BF16 split, 0: FP16 split
     const void* dft;  // DFT matrix image (tc_dft_bytes(N) bytes, prepare_tc_columns)
     int* status;      // set to 1 when an MMA completion wait timed out
+    int skip_mma;     // test hook: issue no MMA and no completion signal (the waits run out)
 };
 bool tc_fft_supported(int N);
 size_t tc_dft_bytes(int N);
 cudaError_t prepare_tc_columns(int N, int bf16, void* dft_dev, cudaStream_t st);
 cudaError_t launch_cols_spectral_tc(int N, int bf16, float2* spec, float2* spec2, float2* edge, const float* kq,
-                                    const float2* tw, const void* dft_dev, float g, int* status, int batch,
-                                    cudaStream_t st);
+                                    const float2* tw, const void* dft_dev, float g, int* status, int skip_mma,
+                                    int batch, cudaStream_t st);
+// Test hook of the device allocations: true when this allocation must fail.
+bool alloc_should_fail();
 // aux/fork/join: an auxiliary stream and two events for the concurrent edge pass;
 // tc: the tensor-core column pass instead of the FP32 one (nullptr: FP32).
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,

@@ -60,17 +60,30 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count));
 }
 
-// Bounded wait for phase `parity` of `mbar`; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, int max_iters) {
-    uint32_t done = 0;
-    for (int it = 0; it < max_iters && !done; ++it) {
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for phase `parity` of `mbar`: non-blocking tests with a short
+// sleep between them, for at most `limit_ns` of wall time (and max_iters
+// tests); false if the phase did not complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, int max_iters,
+                                          uint64_t limit_ns = 200000000ull) {
+    const uint64_t t0 = globaltimer_ns();
+    for (int it = 0; it < max_iters; ++it) {
+        uint32_t done;
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
             : "r"(smem_u32(mbar)), "r"(parity)
             : "memory");
+        if (done) return true;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+        __nanosleep(32);
     }
-    return done != 0;
+    return false;
 }
 
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

@@ -285,6 +285,31 @@ int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, const float
 int cosmos_tile_sort_noalloc(const float* x_dev, const float* y_dev, int64_t n, int32_t lattice_n,
                              int32_t granularity, uint32_t* perm_dev, uint64_t stream);
 
+/* ---- checkpoint / resume ----------------------------------------------------
+ * No counterpart in the reference.  A checkpoint is a header (lattice size,
+ * deposit, force mode, particle count, dt, gravity multiplier, steps taken,
+ * FNV-1a checksum) followed by x, y, xOld, yOld, m in identity order.  Loading
+ * requires the same lattice size, particle count, deposit, dt and gravity
+ * multiplier (COSMOS_ERR_INVALID otherwise, and for a truncated or corrupted
+ * file) and restores the step counter.  Synchronous. */
+int cosmos_pm_checkpoint_save(cosmos_pm* h, const char* path);
+int cosmos_pm_checkpoint_load(cosmos_pm* h, const char* path);
+/* Steps advanced since creation (or since the loaded checkpoint's). */
+int cosmos_pm_steps_taken(cosmos_pm* h, int64_t* steps);
+
+/* ---- test hooks (failure injection without a GPU fault) ----------------------
+ * COSMOS_TEST_FAIL_ALLOC:  the value-th device allocation from now, in any
+ *                          handle, fails with COSMOS_ERR_NOMEM (0: off); h may
+ *                          be NULL.
+ * COSMOS_TEST_TC_SKIP_MMA: (tensor-core force modes) the column pass issues no
+ *                          MMA and no completion signal while value != 0, so
+ *                          its bounded waits run out: the next
+ *                          cosmos_pm_synchronize returns COSMOS_ERR_TIMEOUT and
+ *                          the handle stays usable. */
+#define COSMOS_TEST_FAIL_ALLOC 1
+#define COSMOS_TEST_TC_SKIP_MMA 2
+int cosmos_pm_test_hook(cosmos_pm* h, int32_t hook, int64_t value);
+
 /* Page-locked host memory for the asynchronous readbacks (the reference's
  * cudaMallocHost of frame_h, CosmosCuda.cuh:928-929).  *out = NULL on failure. */
 int cosmos_pm_host_alloc(int64_t bytes, void** out);

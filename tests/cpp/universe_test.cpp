@@ -5,6 +5,7 @@
 // one line "PASS {json}" or "FAIL <reason>".
 //
 //   universe_test <lowAccuracy 0|1>
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -116,13 +117,31 @@ int main(int argc, char** argv) {
 
             Universe<K> manual(kParticles, dev, perf, lowAccuracy, 1234);
             collision(manual);
-            std::vector<float> want(size_t(256) * 256);
+            std::vector<float> want(size_t(256) * 256), later(size_t(256) * 256);
             REQUIRE(cosmos_pm_step(manual.handle(), K - 1) == COSMOS_OK, "manual steps");
             REQUIRE(cosmos_pm_render_frame(manual.handle(), want.data()) == COSMOS_OK, "manual frame");
-            double maxdiff = 0.0;
-            for (size_t i = 0; i < want.size(); ++i) maxdiff = std::fmax(maxdiff, std::fabs(double(want[i]) - first[i]));
-            // float atomics in the deposit may reorder the last bits of a cell
-            REQUIRE(maxdiff <= 1e-4, "worker frame timing matches step(K-1) + render");
+            REQUIRE(cosmos_pm_step(manual.handle(), 1) == COSMOS_OK, "manual step");
+            REQUIRE(cosmos_pm_render_frame(manual.handle(), later.data()) == COSMOS_OK, "manual later frame");
+            // Float atomics may reorder the last bits of a density cell, which
+            // can move a particle across a cell edge one step later, and the
+            // frame's fourth root magnifies a lone particle in an empty cell:
+            // compare typical pixels, and against the frame one step later.
+            std::vector<double> d_want(want.size()), d_later(want.size());
+            for (size_t i = 0; i < want.size(); ++i) {
+                d_want[i] = std::fabs(double(want[i]) - first[i]);
+                d_later[i] = std::fabs(double(later[i]) - first[i]);
+            }
+            auto median = [](std::vector<double> v) {
+                std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+                return v[v.size() / 2];
+            };
+            double mean_want = 0.0, mean_later = 0.0;
+            for (size_t i = 0; i < want.size(); ++i) {
+                mean_want += d_want[i];
+                mean_later += d_later[i];
+            }
+            REQUIRE(median(d_want) <= 1e-5, "worker frame timing matches step(K-1) + render");
+            REQUIRE(mean_want < 0.2 * mean_later, "worker frame is not the frame one step later");
         }
 
         // run the worker, read frames as they come
