@@ -177,7 +177,7 @@ def measured_peak_gbs():
 
 
 # ---- CPU baseline: the reference algorithm restated on the host cores ---------------------
-def cpu_baseline(state, N, cic, dt, budget_s: float, min_steps: int = 2):
+def cpu_baseline(state, N, cic, dt, seconds: float, min_steps: int = 2):
     from oracle import pm_oracle
     threads = os.cpu_count() or 1
     pm_oracle.set_threads(threads)
@@ -186,7 +186,7 @@ def cpu_baseline(state, N, cic, dt, budget_s: float, min_steps: int = 2):
     o.step(s.x, s.y, s.x_old, s.y_old, s.m, 1)  # warm-up (page-in, thread pool)
     n = 0
     t0 = time.perf_counter()
-    while n < min_steps or (time.perf_counter() - t0) < budget_s:
+    while n < min_steps or (time.perf_counter() - t0) < seconds:
         o.step(s.x, s.y, s.x_old, s.y_old, s.m, 1)
         n += 1
     dt_s = time.perf_counter() - t0
@@ -302,7 +302,7 @@ def run_ensemble(args, ws, rank, local):
     if not args.no_cpu_baseline:
         # the reference algorithm on the host cores for the largest simulation (bounded sample)
         j = int(np.argmax(Ps))
-        cb = cpu_baseline(states[j], Ns[j], e["cic"], e["dt"], args.cpu_budget)
+        cb = cpu_baseline(states[j], Ns[j], e["cic"], e["dt"], args.cpu_seconds)
         cb["sample"] = "simulation %d of the ensemble (N=%d, P=%d): " % (j, Ns[j], Ps[j]) + cb["sample"]
     if rank != 0:
         return
@@ -340,7 +340,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--particles", type=int, default=None, help="override the particle count (testing)")
-    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-interval", type=int, default=-1)
     ap.add_argument("--force-mode", choices=["spectral", "gradient", "tc-fp16", "tc-bf16"], default="spectral",
@@ -384,7 +384,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(state, N, cic, dt, args.cpu_budget)
+        cb = cpu_baseline(state, N, cic, dt, args.cpu_seconds)
         # the reference arm: each "step" is a bounded sample of the workload on the host cores
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": P / cb["value"] * 1e3,
@@ -616,7 +616,7 @@ def main():
             ref_gpu = {"unavailable": str(exc)}
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_baseline(state, N, cic, dt, args.cpu_budget)
+        cb = cpu_baseline(state, N, cic, dt, args.cpu_seconds)
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

@@ -69,7 +69,7 @@ struct ColShape {
     static constexpr size_t smem = size_t(B) * LinePad<N>::value * sizeof(cplx_t<T>);
 };
 
-// Register budgets (resident CTAs per SM) of the spectral passes.
+// Register limits (resident CTAs per SM) of the spectral passes.
 #ifndef CPM_COLS_SPECTRAL_MINB
 #define CPM_COLS_SPECTRAL_MINB 3
 #endif
@@ -77,7 +77,7 @@ struct ColShape {
 #define CPM_C2R_SPECTRAL_MINB 2
 #endif
 
-// Minimum resident CTAs per SM for a block size (register budget of launch bounds).
+// Minimum resident CTAs per SM for a block size (register limit of launch bounds).
 template <int NT>
 struct MinBlocks {
     static constexpr int value = NT <= 128 ? 6 : (NT <= 256 ? 4 : (NT <= 512 ? 2 : 1));

@@ -1,7 +1,7 @@
 // Tile-key sort that allocates no device memory.
 //
 // For callers that cannot allocate device memory while they run -- a renderer
-// or simulation host that only owns a fixed device budget, code inside a
+// or simulation host that only owns a fixed amount of device memory, code inside a
 // custom allocator or memory-pool callback, or a real-time loop where an
 // allocation may block on a device-wide synchronisation -- this entry point
 // sorts caller-owned device positions with scratch that lives in a fixed,

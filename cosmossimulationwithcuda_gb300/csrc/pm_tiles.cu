@@ -39,7 +39,7 @@ namespace cpm {
 namespace {
 
 constexpr int kFusedThreads = 256;
-// Optional register budget: resident CTAs per SM the fused kernel must allow.
+// Optional register limit: resident CTAs per SM the fused kernel must allow.
 #ifdef CPM_FUSED_MIN_BLOCKS
 #define CPM_FUSED_BOUNDS __launch_bounds__(kFusedThreads, CPM_FUSED_MIN_BLOCKS)
 #else

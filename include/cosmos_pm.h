@@ -268,7 +268,7 @@ int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, const float
 
 /* ---- tile sort without device allocation ---------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory while they run (a host that owns a fixed device budget, code inside
+ * memory while they run (a host that owns a fixed amount of device memory, code inside
  * an allocator or memory-pool callback, a real-time loop where cudaMalloc may
  * stall on a device-wide synchronisation): writes to perm_dev the stable sort
  * permutation (perm[i] = index of the i-th particle in tile-key order, the

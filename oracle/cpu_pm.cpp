@@ -3,10 +3,9 @@
 // This file is the oracle: it restates, on the host, the algorithm of
 // CosmosCuda.cuh (tugrul512bit/CosmosSimulationWithCuda) for the step
 // deposit -> FFT convolution -> gradient -> gather + integrate, following the
-// reference kernels line by line (citations below).  It is used by the test
-// suite as the checker, by bench.py as the timed CPU baseline, and by
-// __graft_entry__.smoke() as the checker.  Nothing in the product library
-// links it or calls it.
+// reference kernels line by line (citations below).  The test suite and
+// __graft_entry__.smoke() compare the CUDA path against it, and bench.py times
+// it as the CPU baseline.  Nothing in the product library links it or calls it.
 //
 // Two precisions share one template:
 //   * R = double : the FP64 oracle (parity reference for the CUDA path);

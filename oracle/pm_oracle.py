@@ -2,8 +2,8 @@
 
 The oracle restates the reference particle-mesh step (CosmosCuda.cuh,
 tugrul512bit/CosmosSimulationWithCuda) on the host.  Only tests/, bench.py's
-CPU-baseline leg and __graft_entry__.smoke() use it, always as the checker or
-as the timed CPU baseline, never as the product path.
+CPU-baseline leg and __graft_entry__.smoke() use it, always as the expected
+result of a comparison or as the timed CPU baseline, never as the product path.
 """
 from __future__ import annotations
 

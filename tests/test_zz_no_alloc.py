@@ -1,7 +1,7 @@
 """The tile sort that allocates no device memory (cosmos_tile_sort_noalloc).
 
 Some callers cannot allocate device memory while they run -- a host that owns
-a fixed device budget, code inside an allocator callback, a real-time render
+a fixed amount of device memory, code inside an allocator callback, a real-time render
 loop where cudaMalloc may stall.  This entry point sorts caller-owned device
 positions using a fixed scratch array built into the library.  Its permutation
 must equal the one of the allocating sort (cosmos_pm_sort) bit for bit, on
