@@ -21,7 +21,7 @@
 //
 // Shapes: L = 1024 (32 x 32, 4 lines per CTA), 2048 (64 x 32, 4 lines),
 // 4096 (64 x 64, 2 lines).  One CTA holds the DFT matrices, its lines (FP32)
-// and one operand buffer: 80 / 208 / 192 KB of shared memory, 128 tensor-memory
+// and one operand buffer: 89 / 217 / 201 KB of shared memory, 128 tensor-memory
 // columns.  Waits on the MMA completion barrier are bounded (200 ms of wall
 // time); a timeout sets *status and the CTA skips its remaining MMAs.
 #include <cmath>
@@ -52,13 +52,16 @@ struct TcShape {
     static constexpr int F1_BYTES = 2 * KA * KA * 2;                  // hi + lo
     static constexpr int F2_BYTES = SHARED_F ? 0 : 2 * KC * KC * 2;
     static constexpr int D0_BYTES = B * L * 8;
-    static constexpr int OPA = 128 * KA, OPC = RC * KC;
-    static constexpr int OP_ELEMS = OPA > OPC ? OPA : OPC;             // per hi / lo
+    // data operands: core matrices adjacent along K 144 bytes apart (bank spread)
+    static constexpr int LBO_OP = 144;
+    static constexpr int SBO_A = (KA / 8) * LBO_OP, SBO_C = (KC / 8) * LBO_OP;
+    static constexpr int OPA_BYTES = (128 / 8) * SBO_A, OPC_BYTES = (RC / 8) * SBO_C;
+    static constexpr int OP_BYTES = OPA_BYTES > OPC_BYTES ? OPA_BYTES : OPC_BYTES;  // per hi / lo
     static constexpr int OFF_F2 = F1_BYTES;
     static constexpr int OFF_D0 = F1_BYTES + F2_BYTES;
     static constexpr int OFF_OPHI = OFF_D0 + D0_BYTES;
-    static constexpr int OFF_OPLO = OFF_OPHI + OP_ELEMS * 2;
-    static constexpr int SMEM = OFF_OPLO + OP_ELEMS * 2;
+    static constexpr int OFF_OPLO = OFF_OPHI + OP_BYTES;
+    static constexpr int SMEM = OFF_OPLO + OP_BYTES;
     static constexpr int TCOLS = 128;
     static_assert(L1 * L2 == L && KA <= 128 && KC <= 128 && GC * KC <= TCOLS && KA <= TCOLS, "tc shape");
 };
@@ -105,20 +108,31 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
         scale_c = scale_a / float(L1);
     }
 
-    // ---- stage A operand: row r = b*L2 + n2, K = (Re n1 | Im n1) ----
-    for (int idx = tid; idx < 128 * L1; idx += kTcThreads) {
-        const int r = idx & 127, n1 = idx >> 7;
-        const int b = r / L2, n2 = r - b * L2;
-        const float2 v = in(b, n1 * L2 + n2);
-        uint16_t h, l;
-        tc::split16<BF16>(v.x * scale_a, h, l);
-        const int o_re = tc::kmajor_offset(r, n1, S::KA) >> 1;
-        ophi[o_re] = h;
-        oplo[o_re] = l;
-        tc::split16<BF16>(v.y * scale_a, h, l);
-        const int o_im = tc::kmajor_offset(r, L1 + n1, S::KA) >> 1;
-        ophi[o_im] = h;
-        oplo[o_im] = l;
+    // ---- stage A operand: row r = b*L2 + n2, K = (Re n1 | Im n1); a thread
+    // packs 8 consecutive n1 of one row into 16-byte core-matrix rows ----
+    {
+        unsigned char* hib = reinterpret_cast<unsigned char*>(ophi);
+        unsigned char* lob = reinterpret_cast<unsigned char*>(oplo);
+        for (int idx = tid; idx < 128 * (L1 / 8); idx += kTcThreads) {
+            const int r = idx & 127, kb = idx >> 7;
+            const int b = r / L2, n2 = r - b * L2;
+            float re[8], im[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float2 v = in(b, (kb * 8 + j) * L2 + n2);
+                re[j] = v.x * scale_a;
+                im[j] = v.y * scale_a;
+            }
+            uint4 h, l;
+            tc::split16x8<BF16>(re, h, l);
+            const int o_re = tc::kmajor_offset(r, kb * 8, S::LBO_OP, S::SBO_A);
+            *reinterpret_cast<uint4*>(hib + o_re) = h;
+            *reinterpret_cast<uint4*>(lob + o_re) = l;
+            tc::split16x8<BF16>(im, h, l);
+            const int o_im = tc::kmajor_offset(r, L1 + kb * 8, S::LBO_OP, S::SBO_A);
+            *reinterpret_cast<uint4*>(hib + o_im) = h;
+            *reinterpret_cast<uint4*>(lob + o_im) = l;
+        }
     }
     tc::fence_smem_to_async();
     tc::fence_before_sync();
@@ -129,12 +143,16 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
         const uint32_t a_hi = tc::smem_u32(ophi), a_lo = tc::smem_u32(oplo);
         const uint32_t b_hi = tc::smem_u32(f1), b_lo = tc::smem_u32(f1 + S::KA * S::KA * 2);
         uint32_t acc = 0;
+        constexpr int AS = 2 * S::LBO_OP;  // bytes per K = 16 slice of a data operand
         for (int kk = 0; kk < S::KA / 16; ++kk, acc = 1)
-            tc::mma_f16(tmem, tc::smem_desc(a_hi + kk * 256, S::KA), tc::smem_desc(b_hi + kk * 256, S::KA), idesc, acc);
+            tc::mma_f16(tmem, tc::smem_desc(a_hi + kk * AS, S::LBO_OP, S::SBO_A), tc::smem_desc(b_hi + kk * 256, S::KA),
+                        idesc, acc);
         for (int kk = 0; kk < S::KA / 16; ++kk)
-            tc::mma_f16(tmem, tc::smem_desc(a_lo + kk * 256, S::KA), tc::smem_desc(b_hi + kk * 256, S::KA), idesc, 1);
+            tc::mma_f16(tmem, tc::smem_desc(a_lo + kk * AS, S::LBO_OP, S::SBO_A), tc::smem_desc(b_hi + kk * 256, S::KA),
+                        idesc, 1);
         for (int kk = 0; kk < S::KA / 16; ++kk)
-            tc::mma_f16(tmem, tc::smem_desc(a_hi + kk * 256, S::KA), tc::smem_desc(b_lo + kk * 256, S::KA), idesc, 1);
+            tc::mma_f16(tmem, tc::smem_desc(a_hi + kk * AS, S::LBO_OP, S::SBO_A), tc::smem_desc(b_lo + kk * 256, S::KA),
+                        idesc, 1);
         tc::commit(mbar);
     }
     if (!*fail && !tc::mbar_wait(mbar, phase, kTcWaitIters)) {
@@ -161,16 +179,14 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
                 const float2 w = __ldg(tw + ((n2 * k1) & (L - 1)));
                 const float yr = (re[j] * w.x - im[j] * w.y) * rescale;
                 const float yi = (re[j] * w.y + im[j] * w.x) * rescale;
-                const int rc = b * L1 + k1;
-                const int g = rc >> 7, row = rc & 127;
-                const int base = g * 128 * S::KC;
+                const int rc = b * L1 + k1;  // stage C row (groups of 128 follow each other)
                 uint16_t h, l;
                 tc::split16<BF16>(yr, h, l);
-                const int o_re = base + (tc::kmajor_offset(row, n2, S::KC) >> 1);
+                const int o_re = tc::kmajor_offset(rc, n2, S::LBO_OP, S::SBO_C) >> 1;
                 ophi[o_re] = h;
                 oplo[o_re] = l;
                 tc::split16<BF16>(yi, h, l);
-                const int o_im = base + (tc::kmajor_offset(row, L2 + n2, S::KC) >> 1);
+                const int o_im = tc::kmajor_offset(rc, L2 + n2, S::LBO_OP, S::SBO_C) >> 1;
                 ophi[o_im] = h;
                 oplo[o_im] = l;
             }
@@ -183,16 +199,21 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
     if (tid == 0 && !*fail && !skip_mma) {
         const uint32_t idesc = tc::idesc_f16(BF16, 128, S::KC);
         const uint32_t b_hi = tc::smem_u32(f2), b_lo = tc::smem_u32(f2 + S::KC * S::KC * 2);
+        constexpr int AS = 2 * S::LBO_OP;
         for (int g = 0; g < S::GC; ++g) {
             const uint32_t d = tmem + uint32_t(g * S::KC);
-            const uint32_t a_hi = tc::smem_u32(ophi + g * 128 * S::KC), a_lo = tc::smem_u32(oplo + g * 128 * S::KC);
+            const uint32_t gofs = uint32_t(g * 16 * S::SBO_C);  // 128 rows = 16 groups of 8
+            const uint32_t a_hi = tc::smem_u32(ophi) + gofs, a_lo = tc::smem_u32(oplo) + gofs;
             uint32_t acc = 0;
             for (int kk = 0; kk < S::KC / 16; ++kk, acc = 1)
-                tc::mma_f16(d, tc::smem_desc(a_hi + kk * 256, S::KC), tc::smem_desc(b_hi + kk * 256, S::KC), idesc, acc);
+                tc::mma_f16(d, tc::smem_desc(a_hi + kk * AS, S::LBO_OP, S::SBO_C), tc::smem_desc(b_hi + kk * 256, S::KC),
+                            idesc, acc);
             for (int kk = 0; kk < S::KC / 16; ++kk)
-                tc::mma_f16(d, tc::smem_desc(a_lo + kk * 256, S::KC), tc::smem_desc(b_hi + kk * 256, S::KC), idesc, 1);
+                tc::mma_f16(d, tc::smem_desc(a_lo + kk * AS, S::LBO_OP, S::SBO_C), tc::smem_desc(b_hi + kk * 256, S::KC),
+                            idesc, 1);
             for (int kk = 0; kk < S::KC / 16; ++kk)
-                tc::mma_f16(d, tc::smem_desc(a_hi + kk * 256, S::KC), tc::smem_desc(b_lo + kk * 256, S::KC), idesc, 1);
+                tc::mma_f16(d, tc::smem_desc(a_hi + kk * AS, S::LBO_OP, S::SBO_C), tc::smem_desc(b_lo + kk * 256, S::KC),
+                            idesc, 1);
         }
         tc::commit(mbar);
     }

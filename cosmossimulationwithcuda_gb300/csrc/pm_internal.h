@@ -99,7 +99,10 @@ constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's wind
 #define CPM_ITEM_MAX 4096
 #endif
 constexpr int kItemMax = CPM_ITEM_MAX;  // particles per work item
-constexpr int kItemDirect = 256; // items with fewer particles skip the shared windows
+#ifndef CPM_ITEM_DIRECT
+#define CPM_ITEM_DIRECT 256
+#endif
+constexpr int kItemDirect = CPM_ITEM_DIRECT;  // items with fewer particles skip the shared windows
 struct WorkItem {
     int x0, y0;           // window origin (cells): tile origin - kTileHalo
     uint32_t begin, end;  // slot range

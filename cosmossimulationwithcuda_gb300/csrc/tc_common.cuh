@@ -25,14 +25,20 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__
 __host__ __device__ constexpr int kmajor_offset(int r, int k, int K) {
     return (r >> 3) * (K * 16) + (k >> 3) * kLBO + (r & 7) * 16 + (k & 7) * 2;
 }
+// The same layout with any LBO / SBO (multiples of 16 bytes): spacing the
+// core matrices adjacent along K by 144 bytes instead of 128 spreads a warp's
+// writes of one row's K elements over distinct shared-memory banks.
+__host__ __device__ constexpr int kmajor_offset(int r, int k, int lbo, int sbo) {
+    return (r >> 3) * sbo + (k >> 3) * lbo + (r & 7) * 16 + (k & 7) * 2;
+}
 
 // Shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), the
 // descriptor version (1) at bits 46-47, base offset 0, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int K) {
-    const uint32_t sbo = uint32_t(K * 16);
-    return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((kLBO >> 4) & 0x3FFFu) << 16) |
-           (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int lbo, int sbo) {
+    return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t((uint32_t(lbo) >> 4) & 0x3FFFu) << 16) |
+           (uint64_t((uint32_t(sbo) >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
 }
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, int K) { return smem_desc(saddr, kLBO, K * 16); }
 
 // Instruction descriptor, kind::f16: FP32 accumulator, A and B both FP16 or
 // both BF16, both K-major, shape M x N.
@@ -115,6 +121,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // Split v into a 16-bit high part and the 16-bit rounding of the remainder.
+template <int BF16>
+__device__ __forceinline__ void split16(float v, uint16_t& hi, uint16_t& lo);
+
+// Eight values split and packed as two 16-byte rows of a core matrix.
+template <int BF16>
+__device__ __forceinline__ void split16x8(const float (&v)[8], uint4& hi, uint4& lo) {
+    uint16_t h[8], l[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) split16<BF16>(v[j], h[j], l[j]);
+    hi = make_uint4(h[0] | (uint32_t(h[1]) << 16), h[2] | (uint32_t(h[3]) << 16), h[4] | (uint32_t(h[5]) << 16),
+                    h[6] | (uint32_t(h[7]) << 16));
+    lo = make_uint4(l[0] | (uint32_t(l[1]) << 16), l[2] | (uint32_t(l[3]) << 16), l[4] | (uint32_t(l[5]) << 16),
+                    l[6] | (uint32_t(l[7]) << 16));
+}
+
 template <int BF16>
 __device__ __forceinline__ void split16(float v, uint16_t& hi, uint16_t& lo) {
     if (BF16) {
