@@ -115,7 +115,7 @@ def load(path: str | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("COSMOS_PM_LIBRARY") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(f"cosmos_pm CUDA library not built ({path}); run build() first")
     L = ctypes.CDLL(path)
