@@ -109,6 +109,7 @@ struct cosmos_pm {
 
     // display frames (allocated on the first render call)
     int blur_r = 3;
+    bool render_identity = false;  // the weight table is the identity: no blur pass
     float* rkern = nullptr;
     float* blurred = nullptr;
     float* frame[2] = {nullptr, nullptr};
@@ -768,6 +769,7 @@ int ensure_render(cosmos_pm* h) {
     }
     std::vector<float> w(size_t(R) * R);
     cpm::render_weights(R, w.data());
+    h->render_identity = cpm::render_is_identity(R, w.data());
     float* k = nullptr;
     if ((rc = dalloc(&k, w.size()))) return rc;
     if (cudaMemcpy(k, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -783,8 +785,8 @@ int ensure_render(cosmos_pm* h) {
 int enqueue_render(cosmos_pm* h, int s) {
     CPM_TRY(ensure_render(h));
     if (!h->density_valid) CPM_TRY(enqueue_prologue(h, h->stream));
-    CPM_CUDA(cpm::launch_render(h->rho, h->blurred, h->frame[s], h->rkern, h->blur_r, h->N, h->rstate, h->rext,
-                                h->stream));
+    CPM_CUDA(cpm::launch_render(h->rho, h->blurred, h->frame[s], h->rkern, h->blur_r, h->N, h->render_identity,
+                                h->rstate, h->rext, h->stream));
     return COSMOS_OK;
 }
 

@@ -133,8 +133,9 @@ cudaError_t launch_generate(const cosmos_ic_params& p, int64_t count, int64_t fi
 
 // pm_render.cu -- display frame of the density (the reference's render chain)
 void render_weights(int R, float* w);
+bool render_is_identity(int R, const float* w);
 cudaError_t render_init(uint32_t* state, float* extremes, cudaStream_t st);
 cudaError_t launch_render(const float* rho, float* blurred, float* frame, const float* kern, int R, int N,
-                          uint32_t* state, float* extremes, cudaStream_t st);
+                          bool identity, uint32_t* state, float* extremes, cudaStream_t st);
 
 }  // namespace cpm

@@ -17,6 +17,9 @@
 // halo tile and reduces the tile's extremes into order-preserving integer keys
 // with one atomic pair per CTA; the last CTA to finish folds them into the
 // running extremes and re-arms the keys.  k_render_scale applies the power law.
+// When the weight table is the identity (the default BLUR_R = 3: only the
+// centre weight is nonzero) the blurred lattice equals the density, so
+// k_render_minmax takes the extremes of the density and the blur is skipped.
 #include <cfloat>
 
 #include "pm_common.cuh"
@@ -39,42 +42,18 @@ __device__ __forceinline__ float funkey(uint32_t k) {
 
 }  // namespace
 
+// Fold a CTA's (lo, hi) into the frame extremes: one atomic pair per CTA on
+// order-preserving integer keys; the last CTA to finish folds the frame's
+// extremes into the running extremes (k_smoothMinMax) and re-arms the keys.
 // state: [0] min key, [1] max key, [2] finished-CTA counter (uint32);
-// extremes: [0] running min, [1] running max (float)
-__global__ void __launch_bounds__(256) k_render_blur_minmax(const float* __restrict__ rho, float* __restrict__ blurred,
-                                                            const float* __restrict__ kern, int R, int N, int T,
-                                                            uint32_t* __restrict__ state, float* __restrict__ extremes) {
-    extern __shared__ float tile[];
-    const int h = (R - 1) / 2;
-    const int TW = T + 2 * h;
-    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
-    for (int i = threadIdx.x; i < TW * TW; i += blockDim.x) {
-        const int r = i / TW, c = i - r * TW;
-        const int gx = x0 + c - h, gy = y0 + r - h;
-        tile[i] = (gx >= 0 && gx < N && gy >= 0 && gy < N) ? __ldg(rho + size_t(gy) * N + gx) : 0.0f;
-    }
-    __syncthreads();
-    float lo = 0.0f, hi = FLT_MIN;  // the reference's padding and initial maximum
-    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
-        const int ty = i / T, tx = i - ty * T;
-        // two partial sums by column parity, rows outer: the reference's order
-        float a0 = 0.0f, a1 = 0.0f;
-        for (int iy = 0; iy < R; ++iy) {
-            const float* row = tile + (ty + iy) * TW + tx;
-            const float* kr = kern + iy * R;
-            for (int ix = 0; ix < R; ix += 2) a0 = fmaf(row[ix], __ldg(kr + ix), a0);
-            for (int ix = 1; ix < R; ix += 2) a1 = fmaf(row[ix], __ldg(kr + ix), a1);
-        }
-        const float acc = a0 + a1;
-        blurred[size_t(y0 + ty) * N + x0 + tx] = acc;
-        lo = fminf(lo, acc);
-        hi = fmaxf(hi, acc);
-    }
+// extremes: [0] running min, [1] running max (float).
+__device__ __forceinline__ void fold_extremes(float lo, float hi, uint32_t* __restrict__ state,
+                                              float* __restrict__ extremes) {
     for (int off = 16; off > 0; off >>= 1) {
         lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
         hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
     }
-    __shared__ float wlo[8], whi[8];
+    __shared__ float wlo[32], whi[32];
     __shared__ bool last;
     if ((threadIdx.x & 31) == 0) {
         wlo[threadIdx.x >> 5] = lo;
@@ -105,14 +84,67 @@ __global__ void __launch_bounds__(256) k_render_blur_minmax(const float* __restr
     }
 }
 
-__global__ void k_render_scale(const float* __restrict__ blurred, float* __restrict__ frame,
-                               const float* __restrict__ extremes, int64_t n) {
+// Blur with an R x R weight table, one 32 x 32 tile per CTA from a shared
+// halo tile, and the tile's extremes.
+__global__ void __launch_bounds__(256) k_render_blur_minmax(const float* __restrict__ rho, float* __restrict__ blurred,
+                                                            const float* __restrict__ kern, int R, int N, int T,
+                                                            uint32_t* __restrict__ state, float* __restrict__ extremes) {
+    extern __shared__ float tile[];
+    __shared__ float wk[15 * 15];
+    const int h = (R - 1) / 2;
+    const int TW = T + 2 * h;
+    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+    for (int i = threadIdx.x; i < R * R; i += blockDim.x) wk[i] = __ldg(kern + i);
+    for (int i = threadIdx.x; i < TW * TW; i += blockDim.x) {
+        const int r = i / TW, c = i - r * TW;
+        const int gx = x0 + c - h, gy = y0 + r - h;
+        tile[i] = (gx >= 0 && gx < N && gy >= 0 && gy < N) ? __ldg(rho + size_t(gy) * N + gx) : 0.0f;
+    }
+    __syncthreads();
+    float lo = 0.0f, hi = FLT_MIN;  // the reference's padding and initial maximum
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+        const int ty = i / T, tx = i - ty * T;
+        // two partial sums by column parity, rows outer: the reference's order
+        float a0 = 0.0f, a1 = 0.0f;
+        for (int iy = 0; iy < R; ++iy) {
+            const float* row = tile + (ty + iy) * TW + tx;
+            const float* kr = wk + iy * R;
+            for (int ix = 0; ix < R; ix += 2) a0 = fmaf(row[ix], kr[ix], a0);
+            for (int ix = 1; ix < R; ix += 2) a1 = fmaf(row[ix], kr[ix], a1);
+        }
+        const float acc = a0 + a1;
+        blurred[size_t(y0 + ty) * N + x0 + tx] = acc;
+        lo = fminf(lo, acc);
+        hi = fmaxf(hi, acc);
+    }
+    fold_extremes(lo, hi, state, extremes);
+}
+
+// Extremes of an unblurred lattice (the weight table is the identity: with
+// the default BLUR_R = 3 only the centre weight, 1, is nonzero, and the
+// reference's sum 0 + x * 1 + sum of x * 0 is x itself).
+__global__ void __launch_bounds__(512) k_render_minmax(const float4* __restrict__ src, int64_t n4,
+                                                       uint32_t* __restrict__ state, float* __restrict__ extremes) {
+    float lo = 0.0f, hi = FLT_MIN;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += int64_t(gridDim.x) * blockDim.x) {
+        const float4 v = __ldg(src + i);
+        lo = fminf(lo, fminf(fminf(v.x, v.y), fminf(v.z, v.w)));
+        hi = fmaxf(hi, fmaxf(fmaxf(v.x, v.y), fmaxf(v.z, v.w)));
+    }
+    fold_extremes(lo, hi, state, extremes);
+}
+
+__global__ void k_render_scale(const float4* __restrict__ src, float4* __restrict__ frame,
+                               const float* __restrict__ extremes, int64_t n4) {
     const float lo = extremes[0], hi = extremes[1];
     const float diff = hi - lo;
     // The reference is built with fast math, which turns its x / y and powf
     // into these two intrinsics.
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-        frame[i] = 1.8f * __powf(__fdividef(blurred[i] - lo, diff), 0.25f);
+    auto f = [lo, diff](float v) { return 1.8f * __powf(__fdividef(v - lo, diff), 0.25f); };
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n4; i += int64_t(gridDim.x) * blockDim.x) {
+        const float4 v = __ldg(src + i);
+        frame[i] = make_float4(f(v.x), f(v.y), f(v.z), f(v.w));
+    }
 }
 
 // Blur weights of the reference (double r, float weight) for an odd R.
@@ -134,16 +166,32 @@ cudaError_t render_init(uint32_t* state, float* extremes, cudaStream_t st) {
     return e;
 }
 
+bool render_is_identity(int R, const float* w) {
+    const int c = (R / 2) * R + R / 2;
+    for (int i = 0; i < R * R; ++i)
+        if (w[i] != (i == c ? 1.0f : 0.0f)) return false;
+    return true;
+}
+
 cudaError_t launch_render(const float* rho, float* blurred, float* frame, const float* kern, int R, int N,
-                          uint32_t* state, float* extremes, cudaStream_t st) {
-    const int h = (R - 1) / 2;
-    const int T = N < kTile ? N : kTile;  // N is a power of two
-    const size_t smem = size_t(T + 2 * h) * (T + 2 * h) * sizeof(float);
-    k_render_blur_minmax<<<dim3(N / T, N / T), 256, smem, st>>>(rho, blurred, kern, R, N, T, state, extremes);
-    const int64_t n = int64_t(N) * N;
-    int64_t g = (n + 255) / 256;
-    if (g > 4096) g = 4096;
-    k_render_scale<<<int(g), 256, 0, st>>>(blurred, frame, extremes, n);
+                          bool identity, uint32_t* state, float* extremes, cudaStream_t st) {
+    const int64_t n4 = int64_t(N) * N / 4;
+    const float* src = rho;
+    if (identity) {
+        int64_t g = (n4 + 511) / 512;
+        if (g > 608) g = 608;
+        k_render_minmax<<<int(g), 512, 0, st>>>(reinterpret_cast<const float4*>(rho), n4, state, extremes);
+    } else {
+        const int h = (R - 1) / 2;
+        const int T = N < kTile ? N : kTile;  // N is a power of two
+        const size_t smem = size_t(T + 2 * h) * (T + 2 * h) * sizeof(float);
+        k_render_blur_minmax<<<dim3(N / T, N / T), 256, smem, st>>>(rho, blurred, kern, R, N, T, state, extremes);
+        src = blurred;
+    }
+    int64_t g = (n4 + 255) / 256;
+    if (g > 2432) g = 2432;
+    k_render_scale<<<int(g), 256, 0, st>>>(reinterpret_cast<const float4*>(src), reinterpret_cast<float4*>(frame),
+                                          extremes, n4);
     return cudaGetLastError();
 }
 
