@@ -83,9 +83,25 @@ struct MinBlocks {
     static constexpr int value = NT <= 128 ? 6 : (NT <= 256 ? 4 : (NT <= 512 ? 2 : 1));
 };
 
+// Resident CTAs per SM asked of the register allocator: WANT, but no more
+// than SMEM bytes of shared memory per CTA let reside, and never so many that
+// a thread is left fewer than FLOOR registers (a tighter limit only spills:
+// at 4096^2 and 8192^2 the long lines need 512-thread CTAs, which shared
+// memory already holds to one or two per SM).
+template <int NT, size_t SMEM, int WANT, int FLOOR>
+struct FitBlocks {
+    static constexpr int by_regs = 65536 / (NT * FLOOR);
+    static constexpr int by_smem = int((228u * 1024u) / (SMEM + 1024u));
+    static constexpr int v0 = WANT < by_regs ? WANT : by_regs;
+    static constexpr int v1 = v0 < by_smem ? v0 : by_smem;
+    static constexpr int value = v1 < 1 ? 1 : v1;
+};
+
 // ---- pass 1: rows, real -> half spectrum, transposed store --------------------------------
 template <class T, int N, int B, int NT>
-__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(cplx_t<T>),
+                                                 MinBlocks<NT>::value, sizeof(T) == 8 ? 128 : 64>::value))
+    k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
                                                  const cplx_t<T>* __restrict__ tw) {
     using C = cplx_t<T>;
     constexpr int M = N / 2;
@@ -121,7 +137,9 @@ __global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_r2c(const T* 
 // ---- pass 2: columns, forward FFT x K x inverse FFT ----------------------------------------
 // kq: (N/2+1) x (N/2+1) floats, kq[kx*(M+1) + min(ky, N-ky)].
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N>::value * sizeof(float2),
+                                                 MinBlocks<NT>::value, 80>::value))
+    k_cols_conv(float2* __restrict__ spec, const float* __restrict__ kq,
                                                   const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;
@@ -227,7 +245,9 @@ __device__ __forceinline__ void c2r_presplit(float2* s, int lines, const float2*
 // B rows per CTA; the half spectrum is transposed: element (k, row) at
 // spec[k * STRIDE + row].
 template <int N, int B, int NT, int STRIDE = N>
-__global__ void __launch_bounds__(NT, MinBlocks<NT>::value) k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(float2),
+                                                 MinBlocks<NT>::value, 64>::value))
+    k_rows_c2r(const float2* __restrict__ spec, float* __restrict__ out,
                                                  const float2* __restrict__ tw) {
     using C = float2;
     constexpr int M = N / 2;
@@ -301,7 +321,9 @@ __device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
 // (into spec2); and the three y-edge differences of every line,
 // edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, CPM_COLS_SPECTRAL_MINB) k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>::value * sizeof(float2),
+                                                 CPM_COLS_SPECTRAL_MINB, 128>::value))
+    k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
                                                          float2* __restrict__ edge, const float* __restrict__ kq,
                                                          const float2* __restrict__ tw, float g) {
     using C = float2;
@@ -374,7 +396,9 @@ __global__ void __launch_bounds__(NT, CPM_COLS_SPECTRAL_MINB) k_cols_spectral(fl
 // with the x-edge corrections from Phi, written as interleaved (fx, fy).  The
 // y-edge corrections of rows 0, 1, N-2, N-1 follow in k_apply_edge_rows.
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, CPM_C2R_SPECTRAL_MINB) k_rows_c2r_spectral(const float2* __restrict__ spec,
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N / 2>::value * sizeof(float2),
+                                                 CPM_C2R_SPECTRAL_MINB, 128>::value))
+    k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
                                                              float4* __restrict__ force,
                                                              const float2* __restrict__ tw, float g) {
