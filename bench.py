@@ -570,12 +570,12 @@ def main():
     sim.close()
 
     # ---- the metric's second arm: the same step with the tensor-core split FFT ----
-    tc_arm = None
-    if rank == 0 and not args.no_tc_compare and mode == _lib.FORCE_SPECTRAL and N in (1024, 2048, 4096):
+    # FP16 hi/lo split (tc_split_fft) and BF16 hi/lo split (tc_split_fft_bf16)
+    def tc_run(force_mode, precision):
         try:
             tsteps = min(args.steps, 300)
             with _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=sort_interval,
-                                 sort_granularity=sort_gran, force_mode=_lib.FORCE_SPECTRAL_TC_FP16) as ts:
+                                 sort_granularity=sort_gran, force_mode=force_mode) as ts:
                 ts.set_state(state)
                 terr = None
                 if not args.no_force_check:
@@ -591,11 +591,16 @@ def main():
                 rt.record(b, ts.stream())
                 tms = rt.elapsed_ms(a, b) / tsteps
                 ts.synchronize()
-            tc_arm = {"value": P / (tms / 1e3), "unit": UNIT, "ms_per_step": tms, "steps": tsteps,
-                      "force_rel_err_vs_fp64": terr, "precision": "FP16 hi/lo split operands, FP32 accumulate",
-                      "note": "column FFTs (3 of the 5 length-N transforms per step) as tcgen05 GEMMs"}
+            return {"value": P / (tms / 1e3), "unit": UNIT, "ms_per_step": tms, "steps": tsteps,
+                    "force_rel_err_vs_fp64": terr, "precision": precision,
+                    "note": "column FFTs (3 of the 5 length-N transforms per step) as tcgen05 GEMMs"}
         except Exception as exc:
-            tc_arm = {"unavailable": str(exc)}
+            return {"unavailable": str(exc)}
+
+    tc_arm = tc_arm_bf16 = None
+    if rank == 0 and not args.no_tc_compare and mode == _lib.FORCE_SPECTRAL and N in (1024, 2048, 4096):
+        tc_arm = tc_run(_lib.FORCE_SPECTRAL_TC_FP16, "FP16 hi/lo split operands, FP32 accumulate")
+        tc_arm_bf16 = tc_run(_lib.FORCE_SPECTRAL_TC_BF16, "BF16 hi/lo split operands, FP32 accumulate")
 
     # ---- the reference's own step on the same GPU (its kernels + cuFFT) ----
     ref_gpu = None
@@ -624,7 +629,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config,
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches, "stages_ms": stages, "reference_gpu": ref_gpu,
-            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift, "tc_split_fft": tc_arm,
+            "force_rel_err_vs_fp64": force_err, "fp64_drift": drift, "tc_split_fft": tc_arm, "tc_split_fft_bf16": tc_arm_bf16,
             "e2e_positions": e2e_pos}
     print(json.dumps(line), flush=True)
 
