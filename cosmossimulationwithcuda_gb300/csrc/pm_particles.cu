@@ -206,9 +206,12 @@ constexpr int kRsIpt = 16;
 constexpr int kRsTile = kRsThreads * kRsIpt;
 constexpr int kRsWarps = kRsThreads / 32;
 
+#ifndef CPM_RADIX_CTAS_PER_SM
+#define CPM_RADIX_CTAS_PER_SM 4
+#endif
 int radix_grid(int64_t n, int nsm) {
     const int64_t tiles = (n + kRsTile - 1) / kRsTile;
-    int64_t g = 2 * int64_t(nsm > 0 ? nsm : 152);
+    int64_t g = int64_t(CPM_RADIX_CTAS_PER_SM) * (nsm > 0 ? nsm : 152);
     if (g > tiles) g = tiles;
     if (g < 1) g = 1;
     return int(g);
@@ -373,7 +376,32 @@ cudaError_t launch_iota(uint32_t* v, int64_t n, cudaStream_t st) {
 
 __global__ void __launch_bounds__(kThreads) k_permute(ParticleArrays src, ParticleArrays dst,
                                                       const uint32_t* __restrict__ perm, int64_t n) {
-    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(gridDim.x) * kThreads) {
+    // four destinations per thread: 24 independent gathers in flight
+    const int64_t n4 = n / 4;
+    for (int64_t q = blockIdx.x * int64_t(kThreads) + threadIdx.x; q < n4; q += int64_t(gridDim.x) * kThreads) {
+        const uint4 p = __ldg(reinterpret_cast<const uint4*>(perm) + q);
+        const uint32_t pp[4] = {p.x, p.y, p.z, p.w};
+        float4 x, y, xo, yo, m;
+        uint4 id;
+        float* X = &x.x; float* Y = &y.x; float* XO = &xo.x; float* YO = &yo.x; float* Mm = &m.x;
+        uint32_t* ID = &id.x;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            X[j] = __ldg(src.x + pp[j]);
+            Y[j] = __ldg(src.y + pp[j]);
+            XO[j] = __ldg(src.xo + pp[j]);
+            YO[j] = __ldg(src.yo + pp[j]);
+            Mm[j] = __ldg(src.m + pp[j]);
+            ID[j] = __ldg(src.id + pp[j]);
+        }
+        reinterpret_cast<float4*>(dst.x)[q] = x;
+        reinterpret_cast<float4*>(dst.y)[q] = y;
+        reinterpret_cast<float4*>(dst.xo)[q] = xo;
+        reinterpret_cast<float4*>(dst.yo)[q] = yo;
+        reinterpret_cast<float4*>(dst.m)[q] = m;
+        reinterpret_cast<uint4*>(dst.id)[q] = id;
+    }
+    for (int64_t i = n4 * 4 + blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(gridDim.x) * kThreads) {
         const uint32_t p = __ldg(perm + i);
         dst.x[i] = __ldg(src.x + p);
         dst.y[i] = __ldg(src.y + p);
