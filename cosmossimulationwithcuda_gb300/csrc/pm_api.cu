@@ -172,10 +172,11 @@ bool is_spectral(int mode) {
 }
 bool is_tc(int mode) { return mode == COSMOS_FORCE_SPECTRAL_TC_FP16 || mode == COSMOS_FORCE_SPECTRAL_TC_BF16; }
 
-int launch_spectral(cosmos_pm* h, cudaStream_t st) {
+// clear_rho: zero the density behind the row pass (the step clears it for the deposit that follows).
+int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
     CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
                                         h->cfg.gravity_multiplier, st, h->aux_stream, h->fork_ev, h->join_ev, 1,
-                                        is_tc(h->cfg.force_mode) ? &h->tc : nullptr));
+                                        is_tc(h->cfg.force_mode) ? &h->tc : nullptr, clear_rho ? h->rho : nullptr));
     return COSMOS_OK;
 }
 
@@ -183,13 +184,14 @@ int launch_spectral(cosmos_pm* h, cudaStream_t st) {
 // then the reference's edge-clamped stencil.  Spectral mode: the stencil is
 // applied in Fourier space (no potential field is written).  The profiling
 // event between the two halves marks the start of the force pass.
+// Force of the density in rho; rho is zeroed behind the row pass, ready for the deposit.
 int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
     if (is_spectral(h->cfg.force_mode)) {
-        CPM_TRY(launch_spectral(h, st));
+        CPM_TRY(launch_spectral(h, st, true));
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
     } else {
-        CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st));
+        CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st, 1, h->rho));
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
         CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, g, st));
     }
@@ -198,11 +200,10 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
 
 // One step's kernels on stream st (buffer parity `cur`), assuming rho holds the
 // density of the current positions:
-//   FFT convolution rho -> phi, gradient phi -> force, clear rho,
-//   fused gather + update + deposit of the new positions into rho.
+//   FFT convolution rho -> phi, gradient phi -> force (the row pass clears rho
+//   as it reads it), fused gather + update + deposit of the new positions into rho.
 int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     ParticleArrays& p = state(h);
-    const size_t NN = size_t(h->N) * h->N;
     auto rec = [&](int i) -> int {
         if (profile) CPM_CUDA(cudaEventRecord(h->ev[i], st));
         return COSMOS_OK;
@@ -210,7 +211,6 @@ int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     CPM_TRY(rec(kEvFft));
     CPM_TRY(enqueue_force(h, st, profile));
     CPM_TRY(rec(kEvFused));
-    CPM_CUDA(cudaMemsetAsync(h->rho, 0, NN * sizeof(float), st));
     if (h->items_valid)
         CPM_CUDA(cpm::launch_fused_tiles(h->items, h->n_items, p, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->gran,
                                          h->tiles_grid, st));

@@ -88,6 +88,37 @@ inline int ilog2(int64_t v) {
     return l;
 }
 
+// ---- programmatic dependent launch ------------------------------------------------
+// A kernel launched as a dependent may start while the kernel before it in
+// the stream (or graph) finishes: its CTAs are placed as soon as the previous
+// kernel's CTAs have all started and SM room frees up, and they block in
+// dependency_wait() until that kernel has completed and its memory is
+// visible.  Kernels call dependency_wait() before their first global access,
+// so only the launch and CTA placement overlap; allow_dependents() lets the
+// next kernel be placed before this one ends.  Without the launch attribute
+// both are no-ops.  Measured per step: -6 us at 2048^2 (five kernels of 512
+// to 1024 CTAs), +2.4 us at 512^2 (kernels of 128 CTAs), hence the lattice
+// size from which the step's kernels launch as dependents.
+constexpr int kDependentMinN = 1024;
+__device__ __forceinline__ void dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+inline cudaError_t launch_dependent(bool dependent, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                    cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = dependent ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 }  // namespace cpm
 
 // ---- host error plumbing ---------------------------------------------------------

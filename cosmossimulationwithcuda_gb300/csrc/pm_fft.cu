@@ -102,12 +102,14 @@ template <class T, int N, int B, int NT>
 __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(cplx_t<T>),
                                                  MinBlocks<NT>::value, sizeof(T) == 8 ? 128 : 64>::value))
     k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
-                                                 const cplx_t<T>* __restrict__ tw) {
+                                                 const cplx_t<T>* __restrict__ tw, T* clear) {
     using C = cplx_t<T>;
     constexpr int M = N / 2;
     constexpr int LP = LinePad<M>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
+    dependency_wait();
+    allow_dependents();
     const int y0 = int(blockIdx.x) * B;
     in += size_t(blockIdx.y) * N * N;
     spec += size_t(blockIdx.y) * M * N;
@@ -116,6 +118,10 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>:
     auto src = [rows](int line, int i) { return rows[line * M + i]; };
     auto dst = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
     fft_lines<M, B, NT, -1, C, kMaxRadix>(s, src, dst, tw, 2);
+    if (clear) {  // the rows were read (fft_lines ends with a barrier): zero them for the next deposit
+        C* z = reinterpret_cast<C*>(clear + size_t(blockIdx.y) * N * N + size_t(y0) * N);
+        for (int i = threadIdx.x; i < B * M; i += NT) z[i] = cmake<C>(T(0), T(0));
+    }
     // X[k] = (Z[k] + conj Z[M-k])/2 - i/2 W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i/N)
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
@@ -332,6 +338,8 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): phi_hat; [B, 2B): phi_hat * iS
     float* red = reinterpret_cast<float*>(s + 2 * B * LP);
+    dependency_wait();
+    allow_dependents();
     const int kx0 = int(blockIdx.x) * B;
     spec += size_t(blockIdx.y) * M * N;
     spec2 += size_t(blockIdx.y) * M * N;
@@ -409,6 +417,8 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N /
     C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): Fx spectra, [B, 2B): Fy spectra
     float* red = reinterpret_cast<float*>(s + 2 * B * LP);
     __shared__ float dx[B][3];
+    dependency_wait();
+    allow_dependents();
     const int y0 = int(blockIdx.x) * B;
     spec += size_t(blockIdx.y) * M * N;
     spec2 += size_t(blockIdx.y) * M * N;
@@ -480,6 +490,7 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N /
 // y-edge corrections of Fy on rows 0, 1, N-2, N-1 from the three y-edge
 // differences of every column (dy[j * N + x], j = D01, D02, D13).
 __global__ void k_apply_edge_rows(const float* __restrict__ dy, float2* __restrict__ force, int N, float g) {
+    allow_dependents();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= N) return;
     dy += size_t(blockIdx.y) * 3 * N;
@@ -527,10 +538,10 @@ static cudaError_t allow_smem(K kernel, size_t bytes) {
 
 template <int N>
 static cudaError_t conv_passes_n(const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                                 int batch, cudaStream_t st) {
+                                 int batch, cudaStream_t st, float* clear) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
-    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw, clear);
     k_cols_conv<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, CS::smem, st>>>(spec, kq, tw);
     k_rows_c2r<N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(spec, phi, tw);
     return cudaGetLastError();
@@ -544,7 +555,7 @@ static cudaError_t filter_passes_n(const double* g, double2* spec64, double* gha
     cudaError_t e;
     if ((e = allow_smem(k_rows_r2c<double, N, RS::B, RS::NT>, RS::smem)) != cudaSuccess) return e;
     if ((e = allow_smem(k_cols_fwd_real64<N, CS::B, CS::NT>, CS::smem)) != cudaSuccess) return e;
-    k_rows_r2c<double, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(g, spec64, tw64);
+    k_rows_r2c<double, N, RS::B, RS::NT><<<N / RS::B, RS::NT, RS::smem, st>>>(g, spec64, tw64, nullptr);
     k_cols_fwd_real64<N, CS::B, CS::NT><<<(N / 2) / CS::B, CS::NT, CS::smem, st>>>(spec64, ghat, tw64);
     return cudaGetLastError();
 }
@@ -579,26 +590,29 @@ template <int N>
 static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                      const float* kq, float2* force, const float2* tw, float g, int batch,
                                      cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join,
-                                     const SpectralTc* tc) {
+                                     const SpectralTc* tc, float* clear) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
+    const bool dependent = N >= kDependentMinN;
     cudaError_t e;
-    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw);
+    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw, clear);
     if (tc) {
         if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status,
                                          tc->skip_mma, batch, st)) != cudaSuccess)
             return e;
-    } else {
-        k_cols_spectral<N, CS::B, CS::NT><<<dim3((N / 2) / CS::B, batch), CS::NT, SS::col_smem, st>>>(
-            spec, spec2, edge, kq, tw, g);
+    } else if ((e = launch_dependent(dependent, k_cols_spectral<N, CS::B, CS::NT>, dim3((N / 2) / CS::B, batch),
+                                     dim3(CS::NT), SS::col_smem, st, spec, spec2, edge, kq, tw, g)) != cudaSuccess) {
+        return e;
     }
     if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
     k_rows_c2r<N, 1, SS::ENT, 4><<<dim3(3, batch), SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
     if ((e = cudaEventRecord(join, aux)) != cudaSuccess) return e;
-    k_rows_c2r_spectral<N, SS::RB, SS::RNT><<<dim3(N / SS::RB, batch), SS::RNT, SS::row_smem, st>>>(
-        spec, spec2, reinterpret_cast<float4*>(force), tw, g);
+    if ((e = launch_dependent(dependent, k_rows_c2r_spectral<N, SS::RB, SS::RNT>, dim3(N / SS::RB, batch),
+                              dim3(SS::RNT), SS::row_smem, st, spec, spec2, reinterpret_cast<float4*>(force), tw,
+                              g)) != cudaSuccess)
+        return e;
     if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
     k_apply_edge_rows<<<dim3((N + 255) / 256, batch), 256, 0, st>>>(dy, force, N, g);
     return cudaGetLastError();
@@ -629,13 +643,14 @@ cudaError_t prepare_spectral_passes(int N) {
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
                                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch,
-                                  const SpectralTc* tc) {
+                                  const SpectralTc* tc, float* clear) {
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     if (tc && !tc_fft_supported(N)) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join, tc);
+        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join, tc, \
+                                    clear);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:
@@ -670,12 +685,12 @@ cudaError_t prepare_conv_passes(int N) {
 }
 
 cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                               cudaStream_t st, int batch) {
+                               cudaStream_t st, int batch, float* clear) {
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return conv_passes_n<n>(rho, spec, kq, phi, tw, batch, st);
+        return conv_passes_n<n>(rho, spec, kq, phi, tw, batch, st, clear);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:

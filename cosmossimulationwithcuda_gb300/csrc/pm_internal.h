@@ -9,8 +9,10 @@ namespace cpm {
 // pm_fft.cu
 cudaError_t prepare_conv_passes(int N);
 // batch: lattices of size N stored back to back, processed in one launch per pass
+// clear: when not null (the density itself), the row pass zeroes each density
+// row after reading it, ready for the next step's deposit.
 cudaError_t launch_conv_passes(int N, const float* rho, float2* spec, const float* kq, float* phi, const float2* tw,
-                               cudaStream_t st, int batch = 1);
+                               cudaStream_t st, int batch = 1, float* clear = nullptr);
 int conv_launches_per_step();
 int build_filter(int N, int cic, float* kq_dev, float2* tw_dev, cudaStream_t st);
 // Spectral force: density -> force field (interleaved fx, fy) with the
@@ -37,7 +39,7 @@ bool alloc_should_fail();
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
                                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1,
-                                  const SpectralTc* tc = nullptr);
+                                  const SpectralTc* tc = nullptr, float* clear = nullptr);
 int spectral_launches_per_step();
 
 // pm_particles.cu

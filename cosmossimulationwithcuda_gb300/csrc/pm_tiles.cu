@@ -279,6 +279,7 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
     extern __shared__ float4 smem4[];
     float2* fwin = reinterpret_cast<float2*>(smem4);
     uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
+    dependency_wait();
     const uint32_t n_items = *n_items_p;
     const float2* const force0 = force;
     float* const rho0 = rho;
@@ -332,6 +333,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p
     float4* YO = reinterpret_cast<float4*>(p.yo);
     const float4* Mm = reinterpret_cast<const float4*>(p.m);
     const Window w{nullptr, nullptr, 0, 0, 1.0f, 0.0f};
+    dependency_wait();
     for (int64_t g = blockIdx.x * int64_t(kFusedThreads) + threadIdx.x; g < ngroups;
          g += int64_t(gridDim.x) * kFusedThreads) {
         float4 x = __ldcs(X + g), y = __ldcs(Y + g), xo = __ldcs(XO + g), yo = __ldcs(YO + g);
@@ -404,8 +406,8 @@ cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, c
     const size_t smem = tile_window_smem(gran);
 #define CPM_TILES(C, G)                                                                                      \
     if (cic == C && gran == G) {                                                                             \
-        k_fused_tiles<C, G><<<grid, kFusedThreads, smem, st>>>(items, n_items, p, force, rho, N, dt);        \
-        return cudaGetLastError();                                                                           \
+        return launch_dependent(N >= kDependentMinN, k_fused_tiles<C, G>, dim3(grid),                         \
+                                dim3(kFusedThreads), smem, st, items, n_items, p, force, rho, N, dt);        \
     }
     CPM_TILES(0, 4) CPM_TILES(0, 5) CPM_TILES(0, 6) CPM_TILES(1, 4) CPM_TILES(1, 5) CPM_TILES(1, 6)
 #undef CPM_TILES
@@ -419,11 +421,8 @@ cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2
     int64_t g = (ng + kFusedThreads - 1) / kFusedThreads;
     const int64_t cap = int64_t(nsm) * 8;
     if (g > cap) g = cap;
-    if (cic)
-        k_fused_global<1><<<int(g), kFusedThreads, 0, st>>>(p, ng, force, rho, N, dt);
-    else
-        k_fused_global<0><<<int(g), kFusedThreads, 0, st>>>(p, ng, force, rho, N, dt);
-    return cudaGetLastError();
+    return launch_dependent(N >= kDependentMinN, cic ? k_fused_global<1> : k_fused_global<0>, dim3(unsigned(g)),
+                            dim3(kFusedThreads), 0, st, p, ng, force, rho, N, dt);
 }
 
 }  // namespace cpm
