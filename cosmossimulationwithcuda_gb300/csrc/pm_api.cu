@@ -121,6 +121,8 @@ struct cosmos_pm {
 
     bool use_graph = true;
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer parity][tiled]
+    // kGraphSteps steps in one graph, for runs of steps without a sort
+    cudaGraphExec_t graph_multi[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int64_t steps_taken = 0;  // steps advanced since creation (restored by a checkpoint load)
 
     std::string err;
@@ -235,12 +237,15 @@ void state_rewritten(cosmos_pm* h) {
     h->density_valid = false;
 }
 
-int get_graph(cosmos_pm* h, cudaGraphExec_t* out) {
-    cudaGraphExec_t& g = h->graph[h->cur][h->items_valid ? 1 : 0];
+// The step body `steps` times (1 or kGraphSteps) as one graph, cached per
+// buffer parity and tiling.
+int get_graph(cosmos_pm* h, cudaGraphExec_t* out, int steps = 1) {
+    cudaGraphExec_t& g = (steps == 1 ? h->graph : h->graph_multi)[h->cur][h->items_valid ? 1 : 0];
     if (!g) {
         cudaGraph_t graph = nullptr;
         CPM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_step_body(h, h->stream, false);
+        int rc = COSMOS_OK;
+        for (int i = 0; i < steps && rc == COSMOS_OK; ++i) rc = enqueue_step_body(h, h->stream, false);
         const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
         if (rc != COSMOS_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -284,6 +289,25 @@ int enqueue_step(cosmos_pm* h) {
     }
     ++h->steps_since_sort;
     ++h->steps_taken;
+    return COSMOS_OK;
+}
+
+// kGraphSteps steps as one graph launch when none of them sorts, profiles or
+// needs the prologue: the kernels of consecutive steps then follow one
+// another inside the graph (as programmatic dependents from 1024^2 up).
+constexpr int kGraphSteps = 4;
+bool can_enqueue_multi(const cosmos_pm* h, int remaining) {
+    if (!h->use_graph || h->profiling || !h->density_valid || remaining < kGraphSteps) return false;
+    if (h->sort_interval > 0 && (h->sort_due || h->steps_since_sort + kGraphSteps > h->sort_interval)) return false;
+    return true;
+}
+
+int enqueue_multi(cosmos_pm* h) {
+    cudaGraphExec_t g = nullptr;
+    CPM_TRY(get_graph(h, &g, kGraphSteps));
+    CPM_CUDA(cudaGraphLaunch(g, h->stream));
+    h->steps_since_sort += kGraphSteps;
+    h->steps_taken += kGraphSteps;
     return COSMOS_OK;
 }
 
@@ -370,8 +394,10 @@ void destroy_all(cosmos_pm* h) {
         cudaFree(h->stage[i][1]);
         if (h->stage_ready[i]) cudaEventDestroy(h->stage_ready[i]);
         if (h->stage_done[i]) cudaEventDestroy(h->stage_done[i]);
-        for (int j = 0; j < 2; ++j)
+        for (int j = 0; j < 2; ++j) {
             if (h->graph[i][j]) cudaGraphExecDestroy(h->graph[i][j]);
+            if (h->graph_multi[i][j]) cudaGraphExecDestroy(h->graph_multi[i][j]);
+        }
     }
     cudaFree(h->rs.counts);
     cudaFree(h->rkern);
@@ -916,9 +942,11 @@ int cosmos_pm_step(cosmos_pm* h, int32_t nsteps) {
     if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
     if (nsteps < 0) return finish(h, cpm::fail(COSMOS_ERR_INVALID, "nsteps < 0"));
     DeviceGuard g(h->device);
-    for (int i = 0; i < nsteps; ++i) {
-        const int rc = enqueue_step(h);
+    for (int i = 0; i < nsteps;) {
+        const bool multi = can_enqueue_multi(h, nsteps - i);
+        const int rc = multi ? enqueue_multi(h) : enqueue_step(h);
         if (rc != COSMOS_OK) return finish(h, rc);
+        i += multi ? kGraphSteps : 1;
     }
     return COSMOS_OK;
 }

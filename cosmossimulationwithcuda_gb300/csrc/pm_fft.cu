@@ -596,7 +596,9 @@ static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spe
     using SS = SpecShape<N>;
     const bool dependent = N >= kDependentMinN;
     cudaError_t e;
-    k_rows_r2c<float, N, RS::B, RS::NT><<<dim3(N / RS::B, batch), RS::NT, RS::smem, st>>>(rho, spec, tw, clear);
+    if ((e = launch_dependent(dependent, k_rows_r2c<float, N, RS::B, RS::NT>, dim3(N / RS::B, batch), dim3(RS::NT),
+                              RS::smem, st, rho, spec, tw, clear)) != cudaSuccess)
+        return e;
     if (tc) {
         if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status,
                                          tc->skip_mma, batch, st)) != cudaSuccess)

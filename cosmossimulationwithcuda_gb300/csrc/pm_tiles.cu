@@ -280,6 +280,7 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
     float2* fwin = reinterpret_cast<float2*>(smem4);
     uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
     dependency_wait();
+    allow_dependents();
     const uint32_t n_items = *n_items_p;
     const float2* const force0 = force;
     float* const rho0 = rho;
