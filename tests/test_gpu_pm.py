@@ -239,6 +239,32 @@ def test_sorted_and_unsorted_steps_identical_ngp(cosmos_lib):
             np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("mode", ["spectral", "gradient"])
+def test_step_batching_and_dependent_launches_identical_ngp(cosmos_lib, mode):
+    """At 1024^2 the step's kernels launch as programmatic dependents and runs
+    of steps without a sort go out as four-step graphs: step(13) must equal
+    13 single steps and the direct (graph-free) launches bit for bit (NGP,
+    unit masses: every density sum is exact, so the runs are deterministic)."""
+    N, P, dt = 1024, 1 << 18, 0.002
+    fm = cosmos_lib.FORCE_SPECTRAL if mode == "spectral" else cosmos_lib.FORCE_GRADIENT
+    st = ics.uniform(P, N, dt, seed=4)
+    outs = []
+    for use_graph, batched in ((True, True), (True, False), (False, True)):
+        with _sim(cosmos_lib, N, P, False, dt=dt, sort_interval=6, use_graph=use_graph, force_mode=fm) as s:
+            s.set_state(st)
+            if batched:
+                s.step(13)
+            else:
+                for _ in range(13):
+                    s.step(1)
+            assert s.steps_taken() == 13
+            s.synchronize()
+            outs.append(list(s.get_particles()) + [s.get_field(cosmos_lib.FIELD_DENSITY)])
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("cic", [False, True])
 @pytest.mark.parametrize("sort_interval", [0, 1])
 def test_fused_step_deposits_new_positions(cosmos_lib, cic, sort_interval):
