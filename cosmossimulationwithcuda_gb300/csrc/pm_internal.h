@@ -98,7 +98,7 @@ cudaError_t launch_diagnostics(const ParticleArrays& p, int64_t P, const float* 
 // pm_tiles.cu -- tile-ordered fused gather + update + next-step deposit
 constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's window
 #ifndef CPM_ITEM_MAX
-#define CPM_ITEM_MAX 4096
+#define CPM_ITEM_MAX 8192
 #endif
 constexpr int kItemMax = CPM_ITEM_MAX;  // particles per work item
 #ifndef CPM_ITEM_DIRECT

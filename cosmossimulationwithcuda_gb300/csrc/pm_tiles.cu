@@ -16,9 +16,10 @@
 // global loads / float atomics, so the result is correct for any drift.
 // Items with fewer than kItemDirect particles (sparse tiles) skip the windows.
 //
-// Fixed point: an item's deposits are scaled by S = 2^k <= 2^30 / M, M the
+// Fixed point: an item's deposits are scaled by S = 2^k < 2^31 / M, M the
 // summed mass of the item's (non-heavy) particles, so no window cell can
-// overflow; S is a power of two, so unit masses stay exact and the flush
+// overflow (a cell holds at most M * S plus half a unit of rounding per
+// deposit, below 2^31 + 2^15 < 2^32); S is a power of two, so unit masses stay exact and the flush
 // scales back exactly.  Particles heavier than M/128 deposit with global float
 // atomics so that one heavy body cannot coarsen the resolution of the others.
 // (Shared-memory float atomicAdd is a compare-and-swap loop on this
@@ -237,7 +238,7 @@ __device__ __forceinline__ float block_sum_256(float v, float* red) {
     return s;
 }
 
-// Deposit scale of each item: S = 2^k <= 2^30 / M_light, with M_light the mass
+// Deposit scale of each item: S = 2^k < 2^31 / M_light, with M_light the mass
 // of the item's particles no heavier than 1/128 of the item's total mass.
 __global__ void __launch_bounds__(256) k_item_scales(const float* __restrict__ m, WorkItem* __restrict__ items,
                                                      const uint32_t* __restrict__ n_items) {
@@ -256,11 +257,11 @@ __global__ void __launch_bounds__(256) k_item_scales(const float* __restrict__ m
     }
     const float light = block_sum_256(sl, red);
     if (threadIdx.x == 0) {
-        int ex = 30;
+        int ex = 31;
         if (light > 0.0f) {
             int e2;
             frexpf(light * 1.001f, &e2);  // light < 2^e2
-            ex = 30 - e2;
+            ex = 31 - e2;
         }
         ex = ex > 120 ? 120 : (ex < -120 ? -120 : ex);
         items[it].scale = ldexpf(1.0f, ex);
