@@ -89,6 +89,7 @@ struct cosmos_pm {
     cpm::WorkItem* items = nullptr;
     uint32_t* n_items = nullptr;
     size_t max_items = 0;
+    int item_size = cpm::kItemMax;  // particles per work item (work_item_size)
     bool items_valid = false;
     int tiles_grid = 0;
     bool density_valid = false;  // rho holds the density of the current positions
@@ -326,7 +327,7 @@ int sort_now(cosmos_pm* h) {
                                  cudaMemcpyDeviceToDevice, st));
     CPM_CUDA(cpm::launch_permute(src, dst, h->rs.vals[which], h->P, st));
     CPM_CUDA(cpm::launch_build_items(h->rs.keys[which], dst.m, h->Pq, h->N, h->gran, h->tstart, h->tend, h->items,
-                                     h->n_items, h->max_items, st));
+                                     h->n_items, h->max_items, h->item_size, st));
     h->cur ^= 1;
     h->identity_order = false;
     h->pos_valid = false;
@@ -506,7 +507,8 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
             ;
     }
     const int ntiles = (N >> h->gran) * (N >> h->gran);
-    h->max_items = cpm::max_work_items(h->Pq, ntiles);
+    h->item_size = cpm::work_item_size(h->Pq, h->nsm);
+    h->max_items = cpm::max_work_items(h->Pq, ntiles, h->item_size);
     if (rc == COSMOS_OK) {
         const size_t nranges = cpm::tile_range_elems(N, h->gran, 1);
         if ((rc = dalloc(&h->tstart, nranges)) || (rc = dalloc(&h->tend, nranges)) ||

@@ -55,6 +55,7 @@ struct EnsClass {
     uint32_t *tstart = nullptr, *tend = nullptr, *n_items = nullptr;
     cpm::WorkItem* items = nullptr;
     size_t max_items = 0;
+    int item_size = cpm::kItemMax;
     cudaStream_t stream = nullptr, aux = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
 };
@@ -68,6 +69,7 @@ struct cosmos_ensemble {
     std::vector<std::pair<int, int>> where;  // sim -> (class, local index)
     cudaStream_t stream = nullptr;
     cudaEvent_t start = nullptr;
+    int item_size = cpm::kItemMax;  // work-item size of every class (the classes run concurrently)
     bool density_valid = false, sort_due = true;
     int64_t steps_since_sort = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by buffer parity (all classes flip together)
@@ -157,7 +159,8 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
             return rc;
     c.rs.grid = cpm::radix_grid(c.P, e->nsm);
     const size_t nranges = cpm::tile_range_elems(c.N, c.gran, c.nsims);
-    c.max_items = cpm::max_work_items(c.P, int(nranges));
+    c.item_size = e->item_size;
+    c.max_items = cpm::max_work_items(c.P, int(nranges), c.item_size);
     if ((rc = dalloc(&c.off_dev, S + 1)) || (rc = dalloc(&c.pos, Pa)) || (rc = dalloc(&c.rho, S * NN)) ||
         (rc = dalloc(&c.spec, S * NN / 2)) || (rc = dalloc(&c.force, S * NN)) ||
         (rc = dalloc(&c.kq, size_t(c.N / 2 + 1) * (c.N / 2 + 1))) || (rc = dalloc(&c.tw, size_t(c.N))) ||
@@ -235,6 +238,9 @@ int create_impl(const cosmos_ensemble_config* cfg, const int32_t* ns, const int6
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, e->device) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "device query"));
     e->nsm = prop.multiProcessorCount;
+    int64_t total_particles = 0;
+    for (int s = 0; s < S; ++s) total_particles += ps[s];
+    e->item_size = cpm::work_item_size(total_particles, e->nsm);
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&e->start, cudaEventDisableTiming) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "stream creation"));
@@ -274,7 +280,7 @@ int class_sort(cosmos_ensemble* e, EnsClass& c, cudaStream_t st) {
     CPM_CUDA(cpm::launch_radix_sort(c.rs, c.P, c.sort_bits, &which, st));
     CPM_CUDA(cpm::launch_permute(src, dst, c.rs.vals[which], c.P, st));
     CPM_CUDA(cpm::launch_build_items(c.rs.keys[which], dst.m, c.P, c.N, c.gran, c.tstart, c.tend, c.items, c.n_items,
-                                     c.max_items, st, c.nsims));
+                                     c.max_items, c.item_size, st, c.nsims));
     c.cur ^= 1;
     c.identity_order = false;
     c.pos_valid = false;

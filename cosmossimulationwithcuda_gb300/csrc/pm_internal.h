@@ -100,7 +100,8 @@ constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's wind
 #ifndef CPM_ITEM_MAX
 #define CPM_ITEM_MAX 8192
 #endif
-constexpr int kItemMax = CPM_ITEM_MAX;  // particles per work item
+constexpr int kItemMax = CPM_ITEM_MAX;  // particles per work item, at most
+constexpr int kItemMin = 2048;          // and at least (below the largest size)
 #ifndef CPM_ITEM_DIRECT
 #define CPM_ITEM_DIRECT 256
 #endif
@@ -116,13 +117,17 @@ struct WorkItem {
 // Elements of the tile-range arrays (tstart / tend) for nsims simulations.
 size_t tile_range_elems(int N, int gran, int nsims);
 size_t tile_window_smem(int gran);
-size_t max_work_items(int64_t Pq, int ntiles);
+// Work-item size for Pq particles: the largest of kItemMax, kItemMax / 2, ...
+// that still gives about four items per resident CTA (16 per SM), so that the
+// items of a smaller state still spread over the GPU; kItemMin below that.
+int work_item_size(int64_t Pq, int nsm);
+size_t max_work_items(int64_t Pq, int ntiles, int item_size);
 cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid);
 // Builds the work items of the sorted state and their deposit scales (the
 // masses of the sorted particles are read from `m`).
 cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
                                uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
-                               cudaStream_t st, int nsims = 1);
+                               int item_size, cudaStream_t st, int nsims = 1);
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
                                cudaStream_t st);

@@ -354,7 +354,14 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p
 // ---- host side -------------------------------------------------------------------------------
 size_t tile_window_smem(int gran) { return size_t(win_y(gran)) * win_x(gran) * (sizeof(float2) + sizeof(uint32_t)); }
 
-size_t max_work_items(int64_t Pq, int ntiles) { return size_t(Pq / kItemMax) + size_t(ntiles) + 1; }
+int work_item_size(int64_t Pq, int nsm) {
+    const int64_t want = 16 * int64_t(nsm > 0 ? nsm : 152);
+    for (int s = kItemMax; s > kItemMin; s >>= 1)
+        if (Pq / s >= want) return s;
+    return kItemMin;
+}
+
+size_t max_work_items(int64_t Pq, int ntiles, int item_size) { return size_t(Pq / item_size) + size_t(ntiles) + 1; }
 
 template <int CIC, int GRAN>
 static cudaError_t prep_tiles() {
@@ -385,7 +392,7 @@ size_t tile_range_elems(int N, int gran, int nsims) {
 
 cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
                                uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
-                               cudaStream_t st, int nsims) {
+                               int item_size, cudaStream_t st, int nsims) {
     const int t = N >> gran;
     const int stride = t * t + 1;
     const uint32_t ntiles = uint32_t(tile_range_elems(N, gran, nsims));
@@ -397,7 +404,7 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
         if (g > 4096) g = 4096;
         k_tile_ranges<<<int(g), 256, 0, st>>>(sorted_keys, Pq, ntiles, tstart, tend);
     }
-    k_build_items<<<1, 1024, 0, st>>>(tstart, tend, int(ntiles), stride, gran, kItemMax, items, n_items);
+    k_build_items<<<1, 1024, 0, st>>>(tstart, tend, int(ntiles), stride, gran, item_size, items, n_items);
     if (max_items > 0) k_item_scales<<<unsigned(max_items), 256, 0, st>>>(m, items, n_items);
     return cudaGetLastError();
 }
