@@ -117,7 +117,7 @@ extern "C" int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, 
         return COSMOS_OK;
     }
     const int grans[] = {4, 5, 6};
-    const int intervals[] = {8, 16, 32, 64, 0};
+    const int intervals[] = {8, 16, 24, 32, 48, 64, 0};
     float best_t = 0.0f;
     bool any = false;
     for (int gr : grans) {

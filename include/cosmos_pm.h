@@ -253,7 +253,7 @@ int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
  * No counterpart in the reference (its launch shapes are compile-time
  * constants, CosmosCuda.cuh:29-74).  Searches the tile edge of the particle
  * sort (sort_granularity 4, 5, 6: 16, 32, 64 cells) and the re-sort cadence
- * (sort_interval 8, 16, 32, 64, or never) on the caller's own particle state:
+ * (sort_interval 8, 16, 24, 32, 48, 64, or never) on the caller's own particle state:
  * each candidate runs on a temporary handle from the same host state, `steps`
  * graph-launched steps timed with CUDA events after a warm-up that includes
  * its first sort.  *best = *base with the fastest sort_granularity and
