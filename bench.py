@@ -267,6 +267,7 @@ def run_ensemble(args, ws, rank, local):
     ens.synchronize()
     clk.wait_first()
     e0, e1 = rt.event(), rt.event()
+    barrier(ws)
     try:
         rt.record(e0, stream)
         ens.step(steps)
@@ -275,6 +276,7 @@ def run_ensemble(args, ws, rank, local):
     finally:
         clk.__exit__()
     ens.synchronize()
+    ms = max_over_ranks(ms, ws)
     launches = ens.launches_per_step() * steps
     # whole-step algorithmic bytes: fused step 36 B/particle + 16 B/cell; force passes 37 B/cell (spectral:
     # FFT passes; gradient: 25 B/cell of FFT passes + 12 B/cell of stencil)
@@ -299,7 +301,7 @@ def run_ensemble(args, ws, rank, local):
     ens.close()
     del outs
     cb = None
-    if not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         # the reference algorithm on the host cores for the largest simulation (bounded sample)
         j = int(np.argmax(Ps))
         cb = cpu_baseline(states[j], Ns[j], e["cic"], e["dt"], args.cpu_seconds)
@@ -331,6 +333,25 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def barrier(ws: int):
+    """All ranks meet here (no-op for one rank)."""
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value: float, ws: int) -> float:
+    """The largest `value` of all ranks (the timed region's wall time: the job
+    is as slow as its slowest replica)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def main():
@@ -443,9 +464,7 @@ def main():
     sim.synchronize()
     clk.wait_first()
     e0, e1 = rt.event(), rt.event()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    barrier(ws)
     try:
         rt.record(e0, stream)
         sim.step(args.steps)
@@ -454,12 +473,7 @@ def main():
     finally:
         clk.__exit__()
     sim.synchronize()
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws)
     ms_per_step = ms / args.steps
     value = P * args.steps * ws / (ms / 1e3)
     cons1 = conserved()
@@ -620,7 +634,7 @@ def main():
         except Exception as exc:
             ref_gpu = {"unavailable": str(exc)}
     cb = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(state, N, cic, dt, args.cpu_seconds)
     if rank != 0:
         return
