@@ -25,11 +25,17 @@ namespace cpm {
 // Padded shared-memory index: one spare element after every 16.
 __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 
-// Elements per padded line: L + L/16 + 1 (the +1 staggers consecutive lines
-// across banks for the transposed accesses of the real-FFT passes).
+// Elements per padded line: L + L/16 + stagger.  From 1024 points the
+// stagger is 4: consecutive lines start a quarter of a bank row apart
+// (4 float2 = 32 bytes), so that a warp that touches k = 0..32/B-1 of
+// B = 2, 4 or 8 lines at once (the transposed loads and stores of the row
+// passes) hits every bank twice: two wavefronts, the minimum for 256 bytes
+// (a stagger of one element put four lines' elements on the same banks;
+// measured -5% on the 2048^2 force passes).  Shorter lines keep a stagger of
+// one (measured 2% faster at 512^2).
 template <int L>
 struct LinePad {
-    static constexpr int value = L + L / 16 + 1;
+    static constexpr int value = L + L / 16 + (L >= 1024 ? 4 : 1);
 };
 
 template <int L>
