@@ -77,6 +77,7 @@ struct ColShape {
 #define CPM_C2R_SPECTRAL_MINB 2
 #endif
 
+
 // Minimum resident CTAs per SM for a block size (register limit of launch bounds).
 template <int NT>
 struct MinBlocks {
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
 // y-edge corrections of rows 0, 1, N-2, N-1 follow in k_apply_edge_rows.
 template <int N, int B, int NT>
 __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N / 2>::value * sizeof(float2),
-                                                 CPM_C2R_SPECTRAL_MINB, 128>::value))
+                                                 CPM_C2R_SPECTRAL_MINB, (N <= 512 ? 64 : 128)>::value))
     k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
                                                              float4* __restrict__ force,
@@ -572,7 +573,10 @@ struct SpecShape {
     static constexpr int RB0 = RS::B;
     static constexpr size_t row_bytes0 = 2 * size_t(RB0) * LinePad<M>::value * sizeof(float2);
     static constexpr int RB = row_bytes0 > 200 * 1024 ? RB0 / 2 : RB0;  // rows per CTA
-    static constexpr int RNT0 = RB * M / kMaxRadix;
+    // Up to 512^2 one butterfly per thread per stage (2 RB lines; 64 registers
+    // a thread), above that two (128 registers): measured 43 -> 39 us for the
+    // 512^2 force passes, and 83 -> 86 us at 2048^2 the other way round.
+    static constexpr int RNT0 = (N <= 512 ? 2 : 1) * RB * M / kMaxRadix;
     static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
     // two spectra per row, plus block_sum scratch: one slot per warp for each of the 3 * RB edge sums
     static constexpr size_t row_smem =
