@@ -76,6 +76,12 @@ struct ColShape {
 #ifndef CPM_C2R_SPECTRAL_MINB
 #define CPM_C2R_SPECTRAL_MINB 2
 #endif
+// Up to this lattice size the column pass also runs one butterfly per thread
+// (twice the threads, ~90 registers instead of ~155): measured 38.3 -> 36.2 us
+// for the 512^2 force passes, +2% at 1024^2 and +4% at 2048^2.
+#ifndef CPM_COLS_FULL_MAX_N
+#define CPM_COLS_FULL_MAX_N 512
+#endif
 
 
 // Minimum resident CTAs per SM for a block size (register limit of launch bounds).
@@ -329,7 +335,7 @@ __device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
 // edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
 template <int N, int B, int NT>
 __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>::value * sizeof(float2),
-                                                 CPM_COLS_SPECTRAL_MINB, 128>::value))
+                                                 CPM_COLS_SPECTRAL_MINB, (N <= CPM_COLS_FULL_MAX_N ? 64 : 128)>::value))
     k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
                                                          float2* __restrict__ edge, const float* __restrict__ kq,
                                                          const float2* __restrict__ tw, float g) {
@@ -581,7 +587,14 @@ struct SpecShape {
     // two spectra per row, plus block_sum scratch: one slot per warp for each of the 3 * RB edge sums
     static constexpr size_t row_smem =
         2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + size_t(RNT / 32) * 3 * RB * sizeof(float);
-    static constexpr size_t col_smem = 2 * size_t(CS::B) * LinePad<N>::value * sizeof(float2) + (CS::NT / 32) * 6 * 4;
+    // column pass threads of one lattice: one butterfly per thread in the
+    // inverse transforms (2 B lines) up to CPM_COLS_FULL_MAX_N; batches of
+    // lattices keep CS::NT (measured faster for the ensemble's 512^2 class)
+    static constexpr int CNT = N <= CPM_COLS_FULL_MAX_N ? clamp_threads(2 * CS::B * N / kMaxRadix) : CS::NT;
+    static constexpr size_t col_smem_for(int nt) {
+        return 2 * size_t(CS::B) * LinePad<N>::value * sizeof(float2) + size_t(nt / 32) * 6 * 4;
+    }
+    static constexpr size_t col_smem = col_smem_for(CS::NT);
     static constexpr int ENT0 = M / kMaxRadix;
     static constexpr int ENT = ENT0 < 64 ? 64 : (ENT0 > 1024 ? 1024 : ENT0);  // edge-row C2R threads
     static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
@@ -607,6 +620,10 @@ static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spe
         if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status,
                                          tc->skip_mma, batch, st)) != cudaSuccess)
             return e;
+    } else if (batch == 1 && SS::CNT != CS::NT) {
+        if ((e = launch_dependent(dependent, k_cols_spectral<N, CS::B, SS::CNT>, dim3(N / 2 / CS::B), dim3(SS::CNT),
+                                  SS::col_smem_for(SS::CNT), st, spec, spec2, edge, kq, tw, g)) != cudaSuccess)
+            return e;
     } else if ((e = launch_dependent(dependent, k_cols_spectral<N, CS::B, CS::NT>, dim3((N / 2) / CS::B, batch),
                                      dim3(CS::NT), SS::col_smem, st, spec, spec2, edge, kq, tw, g)) != cudaSuccess) {
         return e;
@@ -630,6 +647,7 @@ static cudaError_t prepare_spectral_n() {
     using SS = SpecShape<N>;
     cudaError_t e;
     if ((e = allow_smem(k_cols_spectral<N, CS::B, CS::NT>, SS::col_smem)) != cudaSuccess) return e;
+    if ((e = allow_smem(k_cols_spectral<N, CS::B, SS::CNT>, SS::col_smem_for(SS::CNT))) != cudaSuccess) return e;
     if ((e = allow_smem(k_rows_c2r<N, 1, SS::ENT, 4>, SS::edge_smem)) != cudaSuccess) return e;
     return allow_smem(k_rows_c2r_spectral<N, SS::RB, SS::RNT>, SS::row_smem);
 }
