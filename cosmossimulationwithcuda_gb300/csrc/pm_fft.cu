@@ -37,13 +37,16 @@ namespace cpm {
 
 // ---- launch shapes ------------------------------------------------------------------
 // Launch shapes (chosen by timing variants at 2048^2): radix-16 Stockham
-// stages with one radix-16 butterfly per thread per stage, about 4096 points
-// per row CTA (at least 4 rows, so that the transposed spectrum moves in
-// 32-byte sectors) and one 2048-point line per column CTA, so that 4-6 CTAs
-// are resident per SM and their load / transform / store phases overlap.
-// Below 2048^2 the rows and lines per CTA shrink so that one lattice still
-// spreads over at least 128 CTAs (N/128 rows, N/256 lines).
-// FP64 (filter build) halves the rows to keep shared memory in range.
+// stages with one radix-16 butterfly per thread per stage of the forward
+// transforms, about 4096 points per row CTA (at least 4 rows, so that the
+// transposed spectrum moves in 32-byte sectors) and one 2048-point line per
+// column CTA, so that 2-4 CTAs are resident per SM and their load /
+// transform / store phases overlap; the spectral passes' two inverse
+// transforms per CTA run two butterflies per thread (128 registers), except
+// up to 512^2 (SpecShape).  Below 2048^2 the rows and lines per CTA shrink
+// so that one lattice still spreads over at least 128 CTAs (N/128 rows,
+// N/256 lines).  FP64 (filter build) halves the rows to keep shared memory
+// in range.
 constexpr int kMaxRadix = 16;
 constexpr int ceil_pow2_min(int v, int lo) { return v < lo ? lo : v; }
 constexpr int clamp_threads(int v) { return v < 64 ? 64 : (v > 1024 ? 1024 : v); }
