@@ -29,7 +29,7 @@ EXPORTS = (
     "cosmos_pm_get_positions_async", "cosmos_pm_poll", "cosmos_pm_wait", "cosmos_pm_run_stage",
     "cosmos_pm_get_field", "cosmos_pm_set_field", "cosmos_pm_sort", "cosmos_pm_tile_keys",
     "cosmos_pm_diagnostics", "cosmos_pm_set_profiling", "cosmos_pm_stage_times", "cosmos_pm_stream",
-    "cosmos_pm_launches_per_step", "cosmos_pm_last_error", "cosmos_pm_version",
+    "cosmos_pm_launches_per_step", "cosmos_pm_kernels_launched", "cosmos_pm_last_error", "cosmos_pm_version",
     "cosmos_tile_sort_noalloc", "cosmos_pm_render_frame", "cosmos_pm_get_frame_async",
     "cosmos_pm_host_alloc", "cosmos_pm_host_free", "cosmos_pm_autotune", "cosmos_pm_generate",
     "cosmos_pm_checkpoint_save", "cosmos_pm_checkpoint_load", "cosmos_pm_steps_taken", "cosmos_pm_test_hook",
@@ -142,6 +142,7 @@ def load(path: str | None = None):
         "cosmos_pm_stage_times": (ctypes.c_int, [_vp, _f32p, ctypes.POINTER(i32)]),
         "cosmos_pm_stream": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64)]),
         "cosmos_pm_launches_per_step": (ctypes.c_int, [_vp, ctypes.POINTER(i32)]),
+        "cosmos_pm_kernels_launched": (ctypes.c_int, [_vp, ctypes.POINTER(i64)]),
         "cosmos_pm_last_error": (ctypes.c_char_p, [_vp]),
         "cosmos_pm_version": (ctypes.c_char_p, []),
         "cosmos_tile_sort_noalloc": (ctypes.c_int, [_vp, _vp, i64, i32, i32, _vp, ctypes.c_uint64]),
@@ -371,6 +372,12 @@ class Simulation:
     def launches_per_step(self) -> int:
         n = ctypes.c_int32()
         self._check(self.L.cosmos_pm_launches_per_step(self.h, ctypes.byref(n)))
+        return n.value
+
+    def kernels_launched(self) -> int:
+        """Kernels enqueued since creation (steps, sorts, prologue deposits, renders)."""
+        n = ctypes.c_int64()
+        self._check(self.L.cosmos_pm_kernels_launched(self.h, ctypes.byref(n)))
         return n.value
 
 

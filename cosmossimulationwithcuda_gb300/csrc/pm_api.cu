@@ -125,6 +125,7 @@ struct cosmos_pm {
     // kGraphSteps steps in one graph, for runs of steps without a sort
     cudaGraphExec_t graph_multi[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int64_t steps_taken = 0;  // steps advanced since creation (restored by a checkpoint load)
+    int64_t kernels_enqueued = 0;  // kernel launches enqueued since creation (cosmos_pm_kernels_launched)
 
     std::string err;
 };
@@ -187,6 +188,18 @@ int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
 // then the reference's edge-clamped stencil.  Spectral mode: the stencil is
 // applied in Fourier space (no potential field is written).  The profiling
 // event between the two halves marks the start of the force pass.
+// Kernels of one step: the force passes (the row pass clears the density) and
+// the fused step kernel.
+int step_launches(const cosmos_pm* h) {
+    const int force = is_spectral(h->cfg.force_mode) ? cpm::spectral_launches_per_step()
+                                                     : cpm::conv_launches_per_step() + 1;
+    return force + 1;
+}
+
+// Kernels of one re-sort: keys, identities, 3 per radix pass, permutation,
+// tile ranges, work items, item scales.
+int sort_launches(const cosmos_pm* h) { return 2 + 3 * ((h->sort_bits + 7) / 8) + 4; }
+
 // Force of the density in rho; rho is zeroed behind the row pass, ready for the deposit.
 int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
@@ -269,11 +282,13 @@ int enqueue_step(cosmos_pm* h) {
     if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kEvPrologue], h->stream));
     if (!h->density_valid) {
         CPM_TRY(enqueue_prologue(h, h->stream));
+        h->kernels_enqueued += 1;
         prologue = true;
     }
     if (h->profiling) CPM_CUDA(cudaEventRecord(h->ev[kEvSort], h->stream));
     if (h->sort_interval > 0 && (h->sort_due || h->steps_since_sort >= h->sort_interval)) {
         CPM_TRY(sort_now(h));
+        h->kernels_enqueued += sort_launches(h);
         sorted = true;
     }
     if (h->profiling) {
@@ -290,6 +305,7 @@ int enqueue_step(cosmos_pm* h) {
     }
     ++h->steps_since_sort;
     ++h->steps_taken;
+    h->kernels_enqueued += step_launches(h);
     return COSMOS_OK;
 }
 
@@ -309,6 +325,7 @@ int enqueue_multi(cosmos_pm* h) {
     CPM_CUDA(cudaGraphLaunch(g, h->stream));
     h->steps_since_sort += kGraphSteps;
     h->steps_taken += kGraphSteps;
+    h->kernels_enqueued += int64_t(kGraphSteps) * step_launches(h);
     return COSMOS_OK;
 }
 
@@ -812,9 +829,13 @@ int ensure_render(cosmos_pm* h) {
 // Render the density of the current positions into device frame slot s.
 int enqueue_render(cosmos_pm* h, int s) {
     CPM_TRY(ensure_render(h));
-    if (!h->density_valid) CPM_TRY(enqueue_prologue(h, h->stream));
+    if (!h->density_valid) {
+        CPM_TRY(enqueue_prologue(h, h->stream));
+        h->kernels_enqueued += 1;
+    }
     CPM_CUDA(cpm::launch_render(h->rho, h->blurred, h->frame[s], h->rkern, h->blur_r, h->N, h->render_identity,
                                 h->rstate, h->rext, h->stream));
+    h->kernels_enqueued += 2;  // extremes (with the blur when there is one), power-law scale
     return COSMOS_OK;
 }
 
@@ -1174,10 +1195,13 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream) {
 
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches) {
     if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
-    // force passes + fused step kernel (the density clear is a memset node)
-    const int force = is_spectral(h->cfg.force_mode) ? cpm::spectral_launches_per_step()
-                                                                 : cpm::conv_launches_per_step() + 1;
-    *launches = force + 1;
+    *launches = step_launches(h);
+    return COSMOS_OK;
+}
+
+int cosmos_pm_kernels_launched(cosmos_pm* h, int64_t* launches) {
+    if (!h || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
+    *launches = h->kernels_enqueued;
     return COSMOS_OK;
 }
 

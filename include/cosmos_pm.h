@@ -249,6 +249,11 @@ int cosmos_pm_stream(cosmos_pm* h, uint64_t* stream);
 /* Number of kernel launches one step enqueues (for launch accounting). */
 int cosmos_pm_launches_per_step(cosmos_pm* h, int32_t* launches);
 
+/* Kernels the handle has enqueued since creation: every step's kernels, the
+ * re-sorts, the first-step deposits and the frame renders (for launch
+ * accounting over a region: read it before and after). */
+int cosmos_pm_kernels_launched(cosmos_pm* h, int64_t* launches);
+
 /* ---- autotuning -----------------------------------------------------------
  * No counterpart in the reference (its launch shapes are compile-time
  * constants, CosmosCuda.cuh:29-74).  Searches the tile edge of the particle

@@ -265,6 +265,28 @@ def test_step_batching_and_dependent_launches_identical_ngp(cosmos_lib, mode):
             np.testing.assert_array_equal(a, b)
 
 
+def test_kernel_launch_accounting(cosmos_lib):
+    """kernels_launched counts every enqueued kernel: a plain step adds
+    launches_per_step, a step that re-sorts adds the sort's kernels on top,
+    a four-step graph adds four steps' worth."""
+    N, P = 256, 40_000
+    st = ics.uniform(P, N, 0.002, seed=2)
+    with _sim(cosmos_lib, N, P, True, dt=0.002, sort_interval=8, force_mode=cosmos_lib.FORCE_SPECTRAL) as s:
+        per = s.launches_per_step()
+        assert per == 6  # row R2C, columns, edge C2R, row C2R, edge apply, fused step
+        s.set_state(st)
+        k0 = s.kernels_launched()
+        s.step(1)  # first-step deposit + sort + step
+        k1 = s.kernels_launched()
+        assert k1 - k0 > per + 1
+        s.step(1)
+        assert s.kernels_launched() - k1 == per
+        k2 = s.kernels_launched()
+        s.step(4)  # one four-step graph (no sort inside)
+        assert s.kernels_launched() - k2 == 4 * per
+        s.synchronize()
+
+
 @pytest.mark.parametrize("cic", [False, True])
 @pytest.mark.parametrize("sort_interval", [0, 1])
 def test_fused_step_deposits_new_positions(cosmos_lib, cic, sort_interval):
