@@ -278,7 +278,8 @@ def run_ensemble(args, ws, rank, local):
     ens.synchronize()
     ms = max_over_ranks(ms, ws)
     launches = ens.launches_per_step() * steps
-    # whole-step algorithmic bytes: fused step 36 B/particle + 16 B/cell; force passes 37 B/cell (spectral:
+    # whole-step algorithmic bytes: fused step 36 B/particle + 12 B/cell, density clear (memset) 4 B/cell;
+    # force passes 37 B/cell (spectral:
     # FFT passes; gradient: 25 B/cell of FFT passes + 12 B/cell of stencil)
     cells = float(sum(n * n for n in Ns))
     algo = 36.0 * Ptot + (16.0 + 37.0) * cells
@@ -506,12 +507,13 @@ def main():
     stages["sort_per_sort"] = round(float(acc[4] / max(sorts, 1)), 5)
     # algorithmic bytes per launch (per step for the FFT passes)
     algo = {
-        # read x, y, xOld, yOld, m (20 B), write x, y, xOld, yOld (16 B); density clear 4 B/cell,
-        # force window 8 B/cell, density flush 4 B/cell
-        "fused_step": 36.0 * P + 16.0 * N * N,
-        # gradient mode: r2c rows 4+4, columns 4+1+4 (real K on a quarter: 1 B/cell), c2r rows 4+4;
-        # spectral mode (force straight from the FFT): r2c 4+4, columns 4+1+8, c2r 8+8
-        "fft_conv": (37.0 if args.force_mode != "gradient" else 25.0) * N * N,
+        # read x, y, xOld, yOld, m (20 B), write x, y, xOld, yOld (16 B); force window 8 B/cell,
+        # density flush 4 B/cell (the clear of the density is the row pass's)
+        "fused_step": 36.0 * P + 12.0 * N * N,
+        # gradient mode: r2c rows 4+4+4 (the density read, the half spectrum written, the density
+        # cleared), columns 4+1+4 (real K on a quarter: 1 B/cell), c2r rows 4+4;
+        # spectral mode (force straight from the FFT): r2c 4+4+4, columns 4+1+8, c2r 8+8
+        "fft_conv": (41.0 if args.force_mode != "gradient" else 29.0) * N * N,
         "force": 12.0 * N * N,
     }
     dom = max(algo, key=lambda k: stages.get(k, 0.0))
