@@ -38,6 +38,8 @@ CASES = {
     "cic64_disk": (64, True, 0.01, 4096, 5, "disk", 12),
     "cic128_disk": (128, True, 0.005, 8192, 10, "disk", 13),
     "ngp512_uniform": (512, False, 0.002, 16384, 10, "uniform_rest", 14),
+    # the headline lattice and deposit (particles only: the lattices are 16-32 MB)
+    "cic2048_disk": (2048, True, 0.001, 16384, 3, "disk", 15),
 }
 
 
@@ -114,15 +116,21 @@ def main():
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--render-only", action="store_true",
                     help="remake only the render fixtures; keep the step cases of the manifest")
+    ap.add_argument("--only", default=None,
+                    help="make only this step case; keep the other cases and the render fixtures of the manifest")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
-    manifest = {}
-    if args.render_only:
+    manifest, kept_render = {}, None
+    if args.render_only or args.only:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "manifest.json")) as f:
-            manifest = json.load(f)["cases"]
+            old = json.load(f)
+        manifest = old["cases"]
+        kept_render = old.get("render", {}) if args.only else None
     for name, (N, cic, dt, P, steps, kind, seed) in CASES.items():
         if args.render_only:
             break
+        if args.only and name != args.only:
+            continue
         inp = make_inputs(N, dt, P, kind, seed)
         with ref_oracle.RefGPU(N, cic, dt, P) as ref:
             ref.set_state(_S(inp))
@@ -137,8 +145,10 @@ def main():
         np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
         manifest[name] = dict(N=N, cic=cic, dt=dt, P=P, steps=steps, kind=kind, seed=seed, fields=N <= 128)
         print(name, "ok", flush=True)
-    render = {}
+    render = {} if kept_render is None else kept_render
     for name, (N, frames) in RENDER_CASES.items():
+        if kept_render is not None:
+            break
         cells = render_sample_cells(N)
         values, digests = [], []
         with ref_oracle.RefGPU(N, False, RENDER_DT, 4) as ref:
