@@ -8,7 +8,9 @@ inputs and outputs as tests/golden/<case>.npz:
   after step 1: density, potential, force (the lattices of the first step) and
               x1, y1, x_old1, y_old1
   after `steps`: xk, yk, x_oldk, y_oldk
-and the render chain's frames as tests/golden/render<N>.npz: a sequence of
+(cases of kind "icdisk": inputs from the counter-based generator, not stored;
+outputs at sampled particles `idx`, plus the next step's density and force
+at sampled `cells`), and the render chain's frames as tests/golden/render<N>.npz: a sequence of
 seeded density lattices (render_density) rendered one after another (the
 running min / max carry over), stored as the values at fixed sampled cells;
 the SHA-256 of every full frame goes into the manifest.
@@ -40,7 +42,39 @@ CASES = {
     "ngp512_uniform": (512, False, 0.002, 16384, 10, "uniform_rest", 14),
     # the headline lattice and deposit (particles only: the lattices are 16-32 MB)
     "cic2048_disk": (2048, True, 0.001, 16384, 3, "disk", 15),
+    # the headline lattice at a density where the sorted tiles of the disk's
+    # inner region hold thousands of particles, so the tile-sorted step runs
+    # its shared-window gathers and fixed-point deposits: 2^20 particles on an
+    # exponential disk of scale 200 cells from the counter-based generator
+    # (inputs regenerated bit for bit by oracle/ic_np.py, not stored); the
+    # outputs are stored at sampled particles and cells
+    "cic2048_disk1m": (2048, True, 0.001, 1 << 20, 3, "icdisk", 16),
 }
+SAMPLES = 65536
+
+
+def make_ic_inputs(N, dt, P, seed):
+    """Exponential disk of scale 200 cells at the lattice centre, circular speeds
+    from the enclosed mass plus 5% dispersion, lognormal(0, 0.3) masses of mean
+    ~1, from the platform-independent float32 generator."""
+    from oracle import ic_np
+    x, y, xo, yo, m = ic_np.generate(ic_np.EXP_DISK, P, seed=seed, N=N, dt=dt, center_x=N / 2.0, center_y=N / 2.0,
+                                     scale=200.0, rmax=N / 2.0 - 8.0, mass=float(P), mass_sigma=0.3, spin=1.0,
+                                     dispersion=0.05, g=1.0)
+    return dict(x=x, y=y, x_old=xo, y_old=yo, m=m)
+
+
+def sample_particles(P, seed):
+    h = _splitmix64(np.arange(SAMPLES, dtype=np.uint64) + np.uint64(seed) * np.uint64(1 << 32))
+    return np.unique((h % np.uint64(P)).astype(np.int64))
+
+
+def sample_cells(N, seed):
+    """Cells of the central half of the lattice (where the disk's mass is)."""
+    h = _splitmix64(np.arange(SAMPLES, dtype=np.uint64) + np.uint64(seed) * np.uint64(1 << 33) + np.uint64(1))
+    cx = N // 4 + (h % np.uint64(N // 2)).astype(np.int64)
+    cy = N // 4 + ((h >> np.uint64(32)) % np.uint64(N // 2)).astype(np.int64)
+    return np.unique(cx + cy * N)
 
 
 def make_inputs(N, dt, P, kind, seed):
@@ -131,7 +165,7 @@ def main():
             break
         if args.only and name != args.only:
             continue
-        inp = make_inputs(N, dt, P, kind, seed)
+        inp = make_ic_inputs(N, dt, P, seed) if kind == "icdisk" else make_inputs(N, dt, P, kind, seed)
         with ref_oracle.RefGPU(N, cic, dt, P) as ref:
             ref.set_state(_S(inp))
             ref.step(1)
@@ -139,7 +173,17 @@ def main():
             x1, y1, xo1, yo1 = ref.state()
             ref.step(steps - 1)
             xk, yk, xok, yok = ref.state()
-        out = dict(inp, x1=x1, y1=y1, x_old1=xo1, y_old1=yo1, xk=xk, yk=yk, x_oldk=xok, y_oldk=yok)
+            if kind == "icdisk":  # the lattices of the next step: the density and force of (xk, yk)
+                ref.step(1)
+                dnext, _, fnext = ref.fields()
+        if kind == "icdisk":
+            idx, cells = sample_particles(P, seed), sample_cells(N, seed)
+            pick = lambda a: a[idx]
+            out = dict(idx=idx, x1=pick(x1), y1=pick(y1), x_old1=pick(xo1), y_old1=pick(yo1), xk=pick(xk),
+                       yk=pick(yk), x_oldk=pick(xok), y_oldk=pick(yok), cells=cells,
+                       density_next=dnext.reshape(-1)[cells], force_next=fnext.reshape(-1, 2)[cells])
+        else:
+            out = dict(inp, x1=x1, y1=y1, x_old1=xo1, y_old1=yo1, xk=xk, yk=yk, x_oldk=xok, y_oldk=yok)
         if N <= 128:
             out.update(density=density, potential=potential, force=force)
         np.savez_compressed(os.path.join(args.out, f"{name}.npz"), **out)
