@@ -985,7 +985,10 @@ int cosmos_pm_synchronize(cosmos_pm* h) {
             CPM_CUDA(cudaMemcpy(&st, h->tc_status, sizeof(int), cudaMemcpyDeviceToHost));
             if (st) {
                 CPM_CUDA(cudaMemset(h->tc_status, 0, sizeof(int)));
-                return cpm::fail(COSMOS_ERR_TIMEOUT, "tensor-core column pass: an MMA completion wait timed out");
+                return cpm::fail(COSMOS_ERR_TIMEOUT,
+                                 st >= 2 ? "tensor-core column pass: an MMA completion wait timed out twice; the "
+                                           "CTA's tensor memory was left allocated"
+                                         : "tensor-core column pass: an MMA completion wait timed out");
             }
         }
         return COSMOS_OK;

@@ -23,7 +23,9 @@
 // 4096 (64 x 64, 2 lines).  One CTA holds the DFT matrices, its lines (FP32)
 // and one operand buffer: 89 / 217 / 201 KB of shared memory, 128 tensor-memory
 // columns.  Waits on the MMA completion barrier are bounded (200 ms of wall
-// time); a timeout sets *status and the CTA skips its remaining MMAs.
+// time); a timeout sets *status and the CTA skips its remaining MMAs, and the
+// batch it had committed gets one more bounded wait before tensor memory is
+// freed (a second timeout leaves the columns allocated, *status = 2).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -74,9 +76,13 @@ __device__ __forceinline__ float warp_max(float v) {
 // One complex length-L transform of the CTA's B lines through both MMA stages.
 // in(b, i) gives element i of line b (already conjugated for an inverse),
 // out(b, k, v) receives output k (to be conjugated by the caller for an inverse).
+// A completion wait that runs out sets *fail (the CTA issues no further MMAs)
+// and, when an MMA batch was committed, records its parity in *pending so that
+// the CTA waits for that batch once more before it frees tensor memory.
 template <int L, int BF16, class In, class Out>
 __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint32_t& phase, int* fail,
-                       float* red, const float2* __restrict__ tw, In in, Out out, int* status, int skip_mma) {
+                       int* pending, float* red, const float2* __restrict__ tw, In in, Out out, int* status,
+                       int skip_mma) {
     using S = TcShape<L>;
     constexpr int L1 = S::L1, L2 = S::L2, B = S::B;
     uint16_t* ophi = reinterpret_cast<uint16_t*>(smem + S::OFF_OPHI);
@@ -157,7 +163,8 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
     }
     if (!*fail && !tc::mbar_wait(mbar, phase, kTcWaitIters)) {
         *fail = 1;
-        atomicExch(status, 1);
+        if (!skip_mma) *pending = int(phase);
+        atomicMax(status, 1);
     }
     phase ^= 1u;
     tc::fence_after_sync();
@@ -219,7 +226,8 @@ __device__ void tc_fft(unsigned char* smem, uint32_t tmem, uint64_t* mbar, uint3
     }
     if (!*fail && !tc::mbar_wait(mbar, phase, kTcWaitIters)) {
         *fail = 1;
-        atomicExch(status, 1);
+        if (!skip_mma) *pending = int(phase);
+        atomicMax(status, 1);
     }
     phase ^= 1u;
     tc::fence_after_sync();
@@ -301,6 +309,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int fail;
+    __shared__ int pending;  // parity of a committed MMA batch whose wait ran out (-1: none)
     __shared__ float red[6 * (kTcThreads / 32)];
     const int tid = threadIdx.x, warp = tid >> 5;
     spec += size_t(blockIdx.y) * M * L;
@@ -318,6 +327,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
     }
     if (tid == 0) {
         fail = 0;
+        pending = -1;
         tc::mbar_init(&mbar, 1);
     }
     if (warp == 0) tc::tmem_alloc(&tmem_base, S::TCOLS);
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
 
     // forward FFT over y, in place
     tc_fft<L, BF16>(
-        smem, tmem, &mbar, phase, &fail, red, tw, [d0](int b, int i) { return d0[b * L + i]; },
+        smem, tmem, &mbar, phase, &fail, &pending, red, tw, [d0](int b, int i) { return d0[b * L + i]; },
         [d0](int b, int k, float2 v) { d0[b * L + k] = v; }, status, skip_mma);
 
     // x K (line kx = 0 packs the real spectra of kx = 0 and kx = N/2)
@@ -388,7 +398,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
     // Psi = IFFT(phi_hat * i S g) -> spec2, then Phi = IFFT(phi_hat) -> spec
     float2* out2 = spec2 + size_t(kx0) * L;
     tc_fft<L, BF16>(
-        smem, tmem, &mbar, phase, &fail, red, tw,
+        smem, tmem, &mbar, phase, &fail, &pending, red, tw,
         [d0, tw, g](int b, int i) {
             const float2 v = d0[b * L + i];
             const float S = g * (tw[(2 * i) & (L - 1)].y - 8.0f * tw[i].y) * (1.0f / 6.0f);
@@ -397,10 +407,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_cols_spectral_tc(float2* __re
         [out2](int b, int k, float2 v) { out2[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status, skip_mma);
     float2* out1 = spec + size_t(kx0) * L;
     tc_fft<L, BF16>(
-        smem, tmem, &mbar, phase, &fail, red, tw, [d0](int b, int i) { return cconj(d0[b * L + i]); },
+        smem, tmem, &mbar, phase, &fail, &pending, red, tw, [d0](int b, int i) { return cconj(d0[b * L + i]); },
         [out1](int b, int k, float2 v) { out1[size_t(b) * L + k] = make_float2(v.x, -v.y); }, status, skip_mma);
 
-    if (warp == 0) tc::tmem_dealloc(tmem, S::TCOLS);
+    // Tensor memory is freed only once no MMA can still write it: after a wait
+    // that ran out, the committed batch gets one more bounded wait; if that
+    // runs out too, the columns stay allocated and *status = 2 reports it.
+    if (warp == 0) {
+        bool idle = true;
+        if (pending >= 0) idle = tc::mbar_wait(&mbar, uint32_t(pending), kTcWaitIters);
+        idle = __all_sync(0xffffffffu, idle);
+        if (idle)
+            tc::tmem_dealloc(tmem, S::TCOLS);
+        else if ((tid & 31) == 0)
+            atomicMax(status, 2);
+    }
 }
 
 // ---- host side ---------------------------------------------------------------------------

@@ -36,14 +36,20 @@ std::mutex g_mu;
 uint32_t* g_scratch_ptr[kMaxDevices] = {};
 int g_nsm[kMaxDevices] = {};
 
-// Device address of the scratch array on the current device (set up once per
-// device; the host-side symbol is only a stand-in for it).
-int scratch_for_current_device(uint32_t** out, int* nsm) {
+// Device address of the scratch array on the current device; the host-side
+// symbol is only a stand-in for it.  Outside stream capture the address is
+// looked up on every call (a device reset or a new primary context reloads the
+// module and may move the array); under capture the address of the last
+// uncaptured call on this device is used, so the first call on a device must
+// come before any capture.
+int scratch_for_current_device(cudaStream_t st, uint32_t** out, int* nsm) {
     int dev = -1;
     CPM_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(COSMOS_ERR_INVALID, "device ordinal out of range");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CPM_CUDA(cudaStreamIsCapturing(st, &cs));
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
@@ -52,6 +58,9 @@ int scratch_for_current_device(uint32_t** out, int* nsm) {
         CPM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         g_scratch_ptr[dev] = static_cast<uint32_t*>(p);
         g_nsm[dev] = sms;
+    } else if (!g_scratch_ptr[dev]) {
+        return fail(COSMOS_ERR_STATE, "cosmos_tile_sort_noalloc: the first call on a device must come before any "
+                                      "stream capture");
     }
     *out = g_scratch_ptr[dev];
     *nsm = g_nsm[dev];
@@ -73,7 +82,7 @@ int tile_sort_noalloc(const float* x, const float* y, int64_t n, int N, int gran
     if (n == 0) return COSMOS_OK;
     uint32_t* base = nullptr;
     int nsm = 0;
-    CPM_TRY(scratch_for_current_device(&base, &nsm));
+    CPM_TRY(scratch_for_current_device(st, &base, &nsm));
     RadixScratch rs{};
     rs.keys[0] = base;
     rs.keys[1] = base + kNoAllocMaxParticles;

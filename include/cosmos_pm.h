@@ -281,11 +281,16 @@ int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, const float
  * cudaMalloc / cudaFree: its scratch is a fixed device array of about 16.5 MB
  * that every GPU loading this library keeps until the process exits, sized
  * for COSMOS_NOALLOC_MAX_PARTICLES particles; larger n returns
- * COSMOS_ERR_RANGE.  Work is enqueued on `stream` (a cudaStream_t as an
- * integer, 0 = legacy default stream) and not waited for.  The first call on
- * a device looks up the scratch address on that device: make it before any
- * stream capture.  All calls on a device share the scratch, so calls whose
- * work overlaps on the GPU race; serialise them. */
+ * COSMOS_ERR_RANGE.  All n particles are ordered (cosmos_pm_sort orders
+ * the first 4*floor(P/4) of a handle and leaves the rest in place, so the two
+ * agree only when n is a multiple of 4).  Work is enqueued on `stream` (a
+ * cudaStream_t as an integer, 0 = legacy default stream) and not waited for.
+ * A call outside stream capture looks up the scratch address on the current
+ * device (so a device reset between calls is harmless); a call under capture
+ * uses the address found by the last uncaptured call, so the first call on a
+ * device must come before any stream capture (COSMOS_ERR_STATE otherwise).
+ * All calls on a device share the scratch, so calls whose work overlaps on
+ * the GPU race; serialise them. */
 #define COSMOS_NOALLOC_MAX_PARTICLES (1 << 20)
 int cosmos_tile_sort_noalloc(const float* x_dev, const float* y_dev, int64_t n, int32_t lattice_n,
                              int32_t granularity, uint32_t* perm_dev, uint64_t stream);

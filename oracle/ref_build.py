@@ -9,6 +9,10 @@
   (CosmosSimulationWithCuda.vcxproj); target compute_103a.
 * oracle/_ref/libref_runner.so from oracle/ref_runner.cpp (host C++ against
   the CUDA driver/runtime and cuFFT), built wherever nvcc is available.
+
+The location of the reference tree comes from the environment
+(COSMOS_REFERENCE_ROOT); `make -C oracle ref` sets it to the tree's place in
+the build container.  Without it only the runner is built.
 """
 from __future__ import annotations
 
@@ -20,7 +24,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("COSMOS_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("COSMOS_REFERENCE_ROOT", "")
 RUNNER = os.path.join(OUT, "libref_runner.so")
 
 # (N, dt, gravity multiplier) of the cases the tests and bench use
@@ -43,7 +47,7 @@ def _nvcc() -> str | None:
 
 
 def reference_present() -> bool:
-    return os.path.exists(os.path.join(REFERENCE_ROOT, "CosmosCuda.cuh"))
+    return bool(REFERENCE_ROOT) and os.path.exists(os.path.join(REFERENCE_ROOT, "CosmosCuda.cuh"))
 
 
 def build_ptx(force: bool = False) -> list[str]:

@@ -80,6 +80,26 @@ def test_noalloc_sort_matches_allocating_sort_twice(cosmos_lib):
         np.testing.assert_array_equal(got, pm_oracle.stable_sort_perm(pm_oracle.sort_keys(x, y, N, gran)))
 
 
+def test_noalloc_sorts_every_particle_of_a_ragged_count(cosmos_lib):
+    """n % 4 != 0: the no-alloc sort orders all n particles (the handle's sort
+    leaves the last n % 4 in place), checked against the oracle's stable sort."""
+    L = cosmos_lib.load()
+    cu = _Cuda()
+    N, gran, P = 1024, 5, 700_003
+    x, y = _positions(7, P, N)
+    dx, dy = cu.upload(x), cu.upload(y)
+    dperm = cu.alloc(P * 4)
+    try:
+        rc = L.cosmos_tile_sort_noalloc(dx, dy, P, N, gran, dperm, 0)
+        assert rc == 0, L.cosmos_pm_last_error(None).decode()
+        assert cu.L.cudaDeviceSynchronize() == 0
+        got = cu.download(dperm, np.empty(P, np.uint32))
+    finally:
+        for p in (dx, dy, dperm):
+            cu.L.cudaFree(p)
+    np.testing.assert_array_equal(got, pm_oracle.stable_sort_perm(pm_oracle.sort_keys(x, y, N, gran)))
+
+
 def test_noalloc_rejects_oversize(cosmos_lib):
     L = cosmos_lib.load()
     rc = L.cosmos_tile_sort_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), cosmos_lib.NOALLOC_MAX_PARTICLES + 1,
