@@ -263,6 +263,20 @@ def force_error_vs_fp64(state, N, cic, dt, F_gpu):
     return {"particles": particles, "lattice": lattice, "reference": "FP64 oracle (CPU) on the same positions"}
 
 
+def force_error_series(sim, N, cic, dt, k: int):
+    """Force error of k consecutive steps, each against FP64 on the GPU's own
+    positions (fused_force_error per step): the first step's record, with the
+    per-step series of all k under "series"."""
+    errs = [fused_force_error(sim, N, cic, dt) for _ in range(max(1, k))]
+    out = dict(errs[0])
+    if len(errs) > 1:
+        out["series"] = {"after_steps": [int(e["positions"].split(" steps")[0].split("after ")[-1]) for e in errs],
+                         "particles": [e["particles"] for e in errs], "lattice": [e["lattice"] for e in errs],
+                         "max_particles": max(e["particles"] for e in errs),
+                         "max_lattice": max(e["lattice"] for e in errs)}
+    return out
+
+
 def fused_force_error(sim, N, cic, dt):
     """Force error of the path as it runs: the positions are read back after
     the steps taken so far, one more step is run, and the force field that step
@@ -312,7 +326,7 @@ def run_ensemble(args, ws, rank, local):
     clk.wait_first()
     barrier(ws)
     try:
-        windows = timed_windows(rt, stream, ens.step, steps)
+        windows = timed_windows(rt, stream, ens.step, steps, min_ms=args.min_timed_ms)
     finally:
         clk.__exit__()
     ens.synchronize()
@@ -420,6 +434,11 @@ def main():
                     help="pick the sort granularity / cadence with cosmos_pm_autotune on this state first")
     ap.add_argument("--no-tc-compare", action="store_true",
                     help="skip the tensor-core split-FFT comparison run of the headline metric")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end runs through host buffers")
+    ap.add_argument("--min-timed-ms", type=float, default=MIN_TIMED_MS,
+                    help="device time the timed windows add up to at least (0: one window of --steps)")
+    ap.add_argument("--precision-steps", type=int, default=3,
+                    help="steps whose force is compared with FP64 after the timed region, per force form")
     ap.add_argument("--workload", default=WORKLOAD,
                     help="the headline disk (default), another single-simulation workload "
                          "(uniform-1M-512-ngp, collide-100M-4096-cic, clumpy-1B-8192-cic) or "
@@ -521,7 +540,7 @@ def main():
     barrier(ws)
     k0 = sim.kernels_launched()
     try:
-        windows = timed_windows(rt, stream, sim.step, args.steps)
+        windows = timed_windows(rt, stream, sim.step, args.steps, min_ms=args.min_timed_ms)
         timed_launches = sim.kernels_launched() - k0  # the steps' kernels and the re-sorts among them
     finally:
         clk.__exit__()
@@ -539,12 +558,12 @@ def main():
     # the FP64 oracle computes the force of the same positions.
     force_err = None
     if rank == 0 and not args.no_force_check:
-        force_err = fused_force_error(sim, N, cic, dt)
+        force_err = force_error_series(sim, N, cic, dt, args.precision_steps)
     cons1 = conserved()
     mtot = float(np.sum(state.m, dtype=np.float64))
     # momentum scale ~ sum m|v| (the larger kinetic energy: runs may start at rest)
     pscale = float(np.sqrt(2.0 * mtot * max(cons0["kinetic"], cons1["kinetic"], 1e-300)))
-    drift = {"steps": args.warmup + timed_steps + (1 if force_err else 0), "start": cons0, "end": cons1,
+    drift = {"steps": args.warmup + timed_steps + (max(1, args.precision_steps) if force_err else 0), "start": cons0, "end": cons1,
              "energy_rel": (cons1["energy"] - cons0["energy"]) / abs(cons0["energy"]) if cons0["energy"] else None,
              "momentum_rel": float(np.hypot(cons1["momentum"][0] - cons0["momentum"][0],
                                             cons1["momentum"][1] - cons0["momentum"][1]) / pscale),
@@ -639,14 +658,16 @@ def main():
                          + (f"the display frame ({N}x{N} floats, the reference's output) read back every {R} steps"
                             if frames else f"x, y read back every {R} steps") + "; host link measured at ~192 GB/s")}
 
-    try:
-        e2e = e2e_run(frames=True)
-    except Exception as exc:  # report, never hide
-        e2e = {"value": None, "unit": UNIT, "error": str(exc)}
-    try:
-        e2e_pos = e2e_run(frames=False)
-    except Exception as exc:
-        e2e_pos = {"value": None, "unit": UNIT, "error": str(exc)}
+    e2e = e2e_pos = None
+    if not args.no_e2e:
+        try:
+            e2e = e2e_run(frames=True)
+        except Exception as exc:  # report, never hide
+            e2e = {"value": None, "unit": UNIT, "error": str(exc)}
+        try:
+            e2e_pos = e2e_run(frames=False)
+        except Exception as exc:
+            e2e_pos = {"value": None, "unit": UNIT, "error": str(exc)}
 
     launches = timed_launches
     sim.close()
@@ -660,10 +681,10 @@ def main():
                 ts.set_state(state)
                 ts.step(args.warmup)
                 ts.synchronize()
-                tw = timed_windows(rt, ts.stream(), ts.step, args.steps, min_ms=MIN_TIMED_MS / 2)
+                tw = timed_windows(rt, ts.stream(), ts.step, args.steps, min_ms=args.min_timed_ms / 2)
                 tsteps = args.steps * len(tw)
                 tms = sum(tw) / tsteps
-                terr = None if args.no_force_check else fused_force_error(ts, N, cic, dt)
+                terr = None if args.no_force_check else force_error_series(ts, N, cic, dt, args.precision_steps)
             return {"value": P / (tms / 1e3), "unit": UNIT, "ms_per_step": tms, "steps": tsteps,
                     "force_rel_err_vs_fp64": terr, "precision": precision,
                     "faster_than_plain": bool(tms < ms_per_step),

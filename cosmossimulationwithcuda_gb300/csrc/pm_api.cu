@@ -73,6 +73,7 @@ struct cosmos_pm {
     float* dy = nullptr;      // spectral mode: y-edge differences per column x
     void* tc_dft = nullptr;   // tensor-core modes: DFT matrix image
     int* tc_status = nullptr; // tensor-core modes: MMA wait timeout flag
+    int* wait_status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
     cpm::SpectralTc tc{};
     float* kq = nullptr;
     float2* tw = nullptr;
@@ -124,6 +125,8 @@ struct cosmos_pm {
     cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [buffer parity][tiled]
     // kGraphSteps steps in one graph, for runs of steps without a sort
     cudaGraphExec_t graph_multi[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    // one step with the profiling events recorded between its stages (event nodes)
+    cudaGraphExec_t graph_prof[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int64_t steps_taken = 0;  // steps advanced since creation (restored by a checkpoint load)
     int64_t kernels_enqueued = 0;  // kernel launches enqueued since creation (cosmos_pm_kernels_launched)
 
@@ -176,6 +179,17 @@ bool is_spectral(int mode) {
 }
 bool is_tc(int mode) { return mode == COSMOS_FORCE_SPECTRAL_TC_FP16 || mode == COSMOS_FORCE_SPECTRAL_TC_BF16; }
 
+// A profiling event: under stream capture an external event-record node of
+// the graph being captured (a plain record would only join streams inside
+// the capture), otherwise a plain record.
+cudaError_t record_profile_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return e;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, st);
+}
+
 // clear_rho: zero the density behind the row pass (the step clears it for the deposit that follows).
 int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
     CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
@@ -205,10 +219,10 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
     if (is_spectral(h->cfg.force_mode)) {
         CPM_TRY(launch_spectral(h, st, true));
-        if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
+        if (profile) CPM_CUDA(record_profile_event(h->ev[kEvForce], st));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st, 1, h->rho));
-        if (profile) CPM_CUDA(cudaEventRecord(h->ev[kEvForce], st));
+        if (profile) CPM_CUDA(record_profile_event(h->ev[kEvForce], st));
         CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, g, st));
     }
     return COSMOS_OK;
@@ -221,7 +235,7 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
 int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     ParticleArrays& p = state(h);
     auto rec = [&](int i) -> int {
-        if (profile) CPM_CUDA(cudaEventRecord(h->ev[i], st));
+        if (profile) CPM_CUDA(record_profile_event(h->ev[i], st));
         return COSMOS_OK;
     };
     CPM_TRY(rec(kEvFft));
@@ -229,7 +243,7 @@ int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     CPM_TRY(rec(kEvFused));
     if (h->items_valid)
         CPM_CUDA(cpm::launch_fused_tiles(h->items, h->n_items, p, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->gran,
-                                         h->tiles_grid, st));
+                                         h->tiles_grid, h->wait_status, st));
     else
         CPM_CUDA(cpm::launch_fused_global(p, h->P, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->nsm, st));
     CPM_TRY(rec(kEvEnd));
@@ -252,14 +266,16 @@ void state_rewritten(cosmos_pm* h) {
 }
 
 // The step body `steps` times (1 or kGraphSteps) as one graph, cached per
-// buffer parity and tiling.
-int get_graph(cosmos_pm* h, cudaGraphExec_t* out, int steps = 1) {
-    cudaGraphExec_t& g = (steps == 1 ? h->graph : h->graph_multi)[h->cur][h->items_valid ? 1 : 0];
+// buffer parity and tiling; profile: one step with the stage events recorded
+// as event nodes of the graph.
+int get_graph(cosmos_pm* h, cudaGraphExec_t* out, int steps = 1, bool profile = false) {
+    cudaGraphExec_t& g =
+        (profile ? h->graph_prof : steps == 1 ? h->graph : h->graph_multi)[h->cur][h->items_valid ? 1 : 0];
     if (!g) {
         cudaGraph_t graph = nullptr;
         CPM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         int rc = COSMOS_OK;
-        for (int i = 0; i < steps && rc == COSMOS_OK; ++i) rc = enqueue_step_body(h, h->stream, false);
+        for (int i = 0; i < steps && rc == COSMOS_OK; ++i) rc = enqueue_step_body(h, h->stream, profile);
         const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
         if (rc != COSMOS_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -292,7 +308,13 @@ int enqueue_step(cosmos_pm* h) {
         sorted = true;
     }
     if (h->profiling) {
-        CPM_TRY(enqueue_step_body(h, h->stream, true));
+        if (h->use_graph) {  // the step as it runs (graph-launched), events between its stages
+            cudaGraphExec_t g = nullptr;
+            CPM_TRY(get_graph(h, &g, 1, true));
+            CPM_CUDA(cudaGraphLaunch(g, h->stream));
+        } else {
+            CPM_TRY(enqueue_step_body(h, h->stream, true));
+        }
         h->have_times = true;
         h->prof_sorted = sorted;
         h->prof_prologue = prologue;
@@ -402,6 +424,7 @@ void destroy_all(cosmos_pm* h) {
     cudaFree(h->dy);
     cudaFree(h->tc_dft);
     cudaFree(h->tc_status);
+    cudaFree(h->wait_status);
     cudaFree(h->kq);
     cudaFree(h->tw);
     cudaFree(h->diag);
@@ -415,6 +438,7 @@ void destroy_all(cosmos_pm* h) {
         for (int j = 0; j < 2; ++j) {
             if (h->graph[i][j]) cudaGraphExecDestroy(h->graph[i][j]);
             if (h->graph_multi[i][j]) cudaGraphExecDestroy(h->graph_multi[i][j]);
+            if (h->graph_prof[i][j]) cudaGraphExecDestroy(h->graph_prof[i][j]);
         }
     }
     cudaFree(h->rs.counts);
@@ -529,11 +553,13 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
     if (rc == COSMOS_OK) {
         const size_t nranges = cpm::tile_range_elems(N, h->gran, 1);
         if ((rc = dalloc(&h->tstart, nranges)) || (rc = dalloc(&h->tend, nranges)) ||
-            (rc = dalloc(&h->items, h->max_items)) || (rc = dalloc(&h->n_items, 1)))
+            (rc = dalloc(&h->items, h->max_items)) || (rc = dalloc(&h->n_items, 1)) ||
+            (rc = dalloc(&h->wait_status, 1)))
             ;
     }
     if (rc != COSMOS_OK) return bail(rc);
-    if (cudaMemsetAsync(h->n_items, 0, sizeof(uint32_t), h->stream) != cudaSuccess)
+    if (cudaMemsetAsync(h->n_items, 0, sizeof(uint32_t), h->stream) != cudaSuccess ||
+        cudaMemsetAsync(h->wait_status, 0, sizeof(int), h->stream) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "memset"));
     if (cpm::prepare_tile_kernels(h->gran, h->cic, h->nsm, &h->tiles_grid) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "tile kernel attributes"));
@@ -980,6 +1006,16 @@ int cosmos_pm_synchronize(cosmos_pm* h) {
     auto impl = [&]() -> int {
         CPM_CUDA(cudaStreamSynchronize(h->stream));
         CPM_CUDA(cudaStreamSynchronize(h->copy_stream));
+        {  // a copy wait of a step kernel that gave up
+            int st = 0;
+            CPM_CUDA(cudaMemcpy(&st, h->wait_status, sizeof(int), cudaMemcpyDeviceToHost));
+            if (st) {
+                CPM_CUDA(cudaMemset(h->wait_status, 0, sizeof(int)));
+                return cpm::fail(COSMOS_ERR_TIMEOUT,
+                                 st == 3 ? "a tensor-map load destination was off the 128-byte grid (tile skipped)"
+                                         : "a step kernel's copy wait (bulk or tensor-map load) timed out");
+            }
+        }
         if (h->tc_status) {  // a tensor-core completion wait that gave up
             int st = 0;
             CPM_CUDA(cudaMemcpy(&st, h->tc_status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1237,12 +1273,13 @@ int cosmos_pm_test_hook(cosmos_pm* h, int32_t hook, int64_t value) {
             DeviceGuard g(h->device);
             cudaStreamSynchronize(h->stream);
             h->tc.skip_mma = value != 0;
-            for (auto& row : h->graph)  // captured steps hold the old kernel argument
-                for (auto& gr : row)
-                    if (gr) {
-                        cudaGraphExecDestroy(gr);
-                        gr = nullptr;
-                    }
+            for (auto* set : {&h->graph, &h->graph_multi, &h->graph_prof})  // captured steps hold the old argument
+                for (auto& row : *set)
+                    for (auto& gr : row)
+                        if (gr) {
+                            cudaGraphExecDestroy(gr);
+                            gr = nullptr;
+                        }
             return COSMOS_OK;
         }
         default:

@@ -53,6 +53,7 @@ struct EnsClass {
     float2* tw = nullptr;
     cpm::RadixScratch rs{};
     uint32_t *tstart = nullptr, *tend = nullptr, *n_items = nullptr;
+    int* status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
     cpm::WorkItem* items = nullptr;
     size_t max_items = 0;
     int item_size = cpm::kItemMax;
@@ -126,7 +127,7 @@ void destroy_class(EnsClass& c) {
     for (void* p : {(void*)c.off_dev, (void*)c.pos, (void*)c.rho, (void*)c.spec, (void*)c.phi, (void*)c.force,
                     (void*)c.spec2, (void*)c.edge, (void*)c.dy, (void*)c.kq, (void*)c.tw, (void*)c.rs.keys[0],
                     (void*)c.rs.keys[1], (void*)c.rs.vals[0], (void*)c.rs.vals[1], (void*)c.rs.counts,
-                    (void*)c.tstart, (void*)c.tend, (void*)c.n_items, (void*)c.items})
+                    (void*)c.tstart, (void*)c.tend, (void*)c.n_items, (void*)c.items, (void*)c.status})
         cudaFree(p);
     for (cudaEvent_t ev : {c.fork, c.join, c.done})
         if (ev) cudaEventDestroy(ev);
@@ -167,7 +168,7 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
         (rc = dalloc(&c.rs.keys[0], Pa)) || (rc = dalloc(&c.rs.keys[1], Pa)) || (rc = dalloc(&c.rs.vals[0], Pa)) ||
         (rc = dalloc(&c.rs.vals[1], Pa)) || (rc = dalloc(&c.rs.counts, cpm::radix_counts_elems(c.rs.grid))) ||
         (rc = dalloc(&c.tstart, nranges)) || (rc = dalloc(&c.tend, nranges)) || (rc = dalloc(&c.n_items, 1)) ||
-        (rc = dalloc(&c.items, c.max_items)))
+        (rc = dalloc(&c.items, c.max_items)) || (rc = dalloc(&c.status, 1)))
         return rc;
     if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
         if ((rc = dalloc(&c.spec2, S * NN / 2)) || (rc = dalloc(&c.edge, S * size_t(c.N / 2) * 4)) ||
@@ -190,6 +191,7 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
     CPM_CUDA(cudaMemsetAsync(c.rho, 0, S * NN * sizeof(float), st));
     CPM_CUDA(cudaMemsetAsync(c.force, 0, S * NN * sizeof(float2), st));
     CPM_CUDA(cudaMemsetAsync(c.n_items, 0, sizeof(uint32_t), st));
+    CPM_CUDA(cudaMemsetAsync(c.status, 0, sizeof(int), st));
     CPM_CUDA(cpm::prepare_conv_passes(c.N));
     if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) CPM_CUDA(cpm::prepare_spectral_passes(c.N));
     CPM_CUDA(cpm::prepare_tile_kernels(c.gran, e->cic, e->nsm, &c.tiles_grid));
@@ -312,7 +314,7 @@ int class_body(cosmos_ensemble* e, EnsClass& c) {
     }
     CPM_CUDA(cudaMemsetAsync(c.rho, 0, size_t(c.nsims) * NN * sizeof(float), st));
     CPM_CUDA(cpm::launch_fused_tiles(c.items, c.n_items, c.buf[c.cur], c.force, c.rho, c.N, e->cic, e->cfg.dt, c.gran,
-                                     c.tiles_grid, st));
+                                     c.tiles_grid, c.status, st));
     return COSMOS_OK;
 }
 
@@ -519,6 +521,16 @@ int cosmos_ensemble_synchronize(cosmos_ensemble* e) {
     DeviceGuard g(e->device);
     auto impl = [&]() -> int {
         CPM_CUDA(cudaStreamSynchronize(e->stream));
+        for (auto& c : e->classes) {  // a copy wait of a step kernel that gave up
+            int st = 0;
+            CPM_CUDA(cudaMemcpy(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost));
+            if (st) {
+                CPM_CUDA(cudaMemset(c.status, 0, sizeof(int)));
+                return cpm::fail(COSMOS_ERR_TIMEOUT,
+                                 st == 3 ? "a tensor-map load destination was off the 128-byte grid (tile skipped)"
+                                         : "a step kernel's copy wait (bulk or tensor-map load) timed out");
+            }
+        }
         return COSMOS_OK;
     };
     return finish(e, impl());

@@ -128,9 +128,11 @@ cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid);
 cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int64_t Pq, int N, int gran,
                                uint32_t* tstart, uint32_t* tend, WorkItem* items, uint32_t* n_items, size_t max_items,
                                int item_size, cudaStream_t st, int nsims = 1);
+// status: a bounded wait of the kernel that ran out sets *status (1: a wait
+// timed out; 2: copies were still in flight when the CTA gave up).
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
-                               cudaStream_t st);
+                               int* status, cudaStream_t st);
 cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
                                 float dt, int nsm, cudaStream_t st);
 

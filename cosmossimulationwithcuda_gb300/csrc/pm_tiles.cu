@@ -31,6 +31,7 @@
 // gather (:231-312) as separate passes.
 #include <cfloat>
 
+#include "bulk_copy.cuh"
 #include "pm_common.cuh"
 #include "pm_internal.h"
 #include "pm_particle_math.cuh"
@@ -324,6 +325,169 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
     }
 }
 
+// ---- the fused step kernel, tile windows, particles staged by bulk copies -----------------
+// Same work as k_fused_tiles, with the particle arrays streamed into shared
+// memory by the SM's bulk-copy engine instead of per-thread loads: one
+// producer warp walks the CTA's work items in order and, per chunk of
+// kBulkChunk particles (the 16-byte-aligned part of an item), copies the five
+// arrays x, y, xOld, yOld, m into one of kBulkStages shared stages; eight
+// consumer warps take one float4 group of each array per thread from the
+// stage (conflict-free 16-byte shared loads), gather, update and deposit as
+// before, and store the new state straight to global memory.  The copies of
+// the next chunks (and of the next item's first chunks) are in flight while a
+// chunk is computed, without holding registers, and the consumer warps of one
+// CTA synchronise among themselves (named barrier) only around the windows.
+// Waits are bounded: a timeout sets *status, the CTA stops issuing work,
+// every warp keeps its barrier schedule with the work skipped, and the
+// producer waits (bounded) for its copies in flight before the CTA exits.
+constexpr int kBulkConsumers = 256;                    // 8 compute warps
+constexpr int kBulkThreads = kBulkConsumers + 32;      // + 1 producer warp
+constexpr int kBulkChunk = 4 * kBulkConsumers;         // particles per stage: one float4 group per thread
+constexpr int kBulkStages = 2;
+constexpr int kBulkArrays = 5;                         // x, y, xOld, yOld, m
+constexpr size_t kBulkStageFloats = size_t(kBulkArrays) * kBulkChunk;
+
+template <int CIC, int GRAN>
+__global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkItem* __restrict__ items,
+                                                                  const uint32_t* __restrict__ n_items_p,
+                                                                  ParticleArrays p, const float2* __restrict__ force,
+                                                                  float* __restrict__ rho, int N, float dt,
+                                                                  int* __restrict__ status) {
+    constexpr int WY = win_y(GRAN), WX = win_x(GRAN);
+    extern __shared__ float4 smem4[];
+    float* stages = reinterpret_cast<float*>(smem4);  // [stage][array][kBulkChunk]
+    float2* fwin = reinterpret_cast<float2*>(stages + kBulkStages * kBulkStageFloats);
+    uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
+    __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
+    __shared__ volatile int abort_flag;
+    const int tid = int(threadIdx.x), warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < kBulkStages; ++s) {
+            bulk::mbar_init(&full[s], 1);
+            bulk::mbar_init(&empty[s], kBulkConsumers / 32);
+        }
+        abort_flag = 0;
+        bulk::fence_barrier_init();
+    }
+    __syncthreads();
+    dependency_wait();
+    allow_dependents();
+    const uint32_t n_items = *n_items_p;
+
+    if (warp == kBulkConsumers / 32) {  // ---- producer warp: one lane issues the copies ----
+        if (lane != 0) return;
+        float* const arr[kBulkArrays] = {p.x, p.y, p.xo, p.yo, p.m};
+        uint32_t fills[kBulkStages] = {};
+        uint32_t fill = 0;
+        for (uint32_t it = blockIdx.x; it < n_items && !abort_flag; it += gridDim.x) {
+            const WorkItem item = items[it];
+            const uint32_t b4 = (item.begin + 3u) & ~3u, e4 = item.end & ~3u;
+            for (uint32_t c = b4; c < e4 && !abort_flag; c += kBulkChunk, ++fill) {
+                const uint32_t n = e4 - c < uint32_t(kBulkChunk) ? e4 - c : uint32_t(kBulkChunk);
+                const int s = int(fill % kBulkStages);
+                if (fills[s] > 0 && !bulk::wait(&empty[s], (fills[s] - 1u) & 1u)) {
+                    abort_flag = 1;
+                    atomicMax(status, 1);
+                    break;
+                }
+                bulk::arrive_expect_tx(&full[s], n * 4u * kBulkArrays);
+                float* st = stages + size_t(s) * kBulkStageFloats;
+#pragma unroll
+                for (int a = 0; a < kBulkArrays; ++a) bulk::copy_g2s(st + a * kBulkChunk, arr[a] + c, n * 4u, &full[s]);
+                ++fills[s];
+            }
+        }
+        // copies still in flight (only after a timeout) must land before the CTA's shared memory goes away
+        for (int s = 0; s < kBulkStages; ++s)
+            if (fills[s] > 0 && !bulk::wait(&full[s], (fills[s] - 1u) & 1u)) atomicMax(status, 2);
+        return;
+    }
+
+    // ---- consumer warps ----
+    const float2* const force0 = force;
+    float* const rho0 = rho;
+    uint32_t use = 0;
+    for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const WorkItem item = items[it];
+        force = force0 + size_t(item.sim) * N * N;
+        rho = rho0 + size_t(item.sim) * N * N;
+        const bool dense = item.end - item.begin >= uint32_t(kItemDirect);
+        if (dense) {
+            for (int i = tid; i < WY * WX; i += kBulkConsumers) {
+                const int r = i / WX, c = i - r * WX;
+                const int gx = item.x0 + c, gy = item.y0 + r;
+                float2 f = make_float2(0.0f, 0.0f);
+                if (gx >= 0 && gx < N && gy >= 0 && gy < N) f = __ldg(force + size_t(gy) * N + gx);
+                fwin[i] = f;
+                dwin[i] = 0u;
+            }
+            bulk::named_sync(kBulkConsumers);
+        }
+        const Window w = dense ? Window{fwin, dwin, item.x0, item.y0, item.scale, item.heavy}
+                               : Window{nullptr, nullptr, item.x0, item.y0, 1.0f, 0.0f};
+        const uint32_t b = item.begin, e = item.end;
+        const uint32_t b4 = (b + 3u) & ~3u, e4 = e & ~3u;
+        if (!abort_flag) {  // ragged head / tail (or the whole range when it spans no full group)
+            const uint32_t h_end = b4 < e ? b4 : e;
+            const uint32_t t_beg = e4 > h_end ? e4 : h_end;
+            const uint32_t nh = h_end - b, nt = e - t_beg;
+            if (uint32_t(tid) < nh + nt) {
+                const uint32_t i = uint32_t(tid) < nh ? b + tid : t_beg + (tid - nh);
+                float px = p.x[i], py = p.y[i], pxo = p.xo[i], pyo = p.yo[i];
+                step_particle<CIC, WX, WY>(px, py, pxo, pyo, p.m[i], w, force, rho, N, dt);
+                p.x[i] = px;
+                p.y[i] = py;
+                p.xo[i] = pxo;
+                p.yo[i] = pyo;
+            }
+        }
+        for (uint32_t c = b4; c < e4; c += kBulkChunk, ++use) {
+            const uint32_t n = e4 - c < uint32_t(kBulkChunk) ? e4 - c : uint32_t(kBulkChunk);
+            const int s = int(use % kBulkStages);
+            bool ok = !abort_flag;
+            if (ok && !bulk::wait(&full[s], (use / kBulkStages) & 1u)) {
+                abort_flag = 1;
+                atomicMax(status, 1);
+                ok = false;
+            }
+            if (ok && uint32_t(4 * tid) < n) {
+                const float4* st = reinterpret_cast<const float4*>(stages + size_t(s) * kBulkStageFloats);
+                constexpr int A4 = kBulkChunk / 4;
+                float4 x = st[tid], y = st[A4 + tid], xo = st[2 * A4 + tid], yo = st[3 * A4 + tid];
+                const float4 m = st[4 * A4 + tid];
+                step_particle<CIC, WX, WY>(x.x, y.x, xo.x, yo.x, m.x, w, force, rho, N, dt);
+                step_particle<CIC, WX, WY>(x.y, y.y, xo.y, yo.y, m.y, w, force, rho, N, dt);
+                step_particle<CIC, WX, WY>(x.z, y.z, xo.z, yo.z, m.z, w, force, rho, N, dt);
+                step_particle<CIC, WX, WY>(x.w, y.w, xo.w, yo.w, m.w, w, force, rho, N, dt);
+                const uint32_t g = (c >> 2) + uint32_t(tid);
+                __stcs(reinterpret_cast<float4*>(p.x) + g, x);
+                __stcs(reinterpret_cast<float4*>(p.y) + g, y);
+                __stcs(reinterpret_cast<float4*>(p.xo) + g, xo);
+                __stcs(reinterpret_cast<float4*>(p.yo) + g, yo);
+            }
+            __syncwarp();
+            if (lane == 0) bulk::arrive(&empty[s]);
+        }
+        if (dense) {
+            bulk::named_sync(kBulkConsumers);
+            constexpr int W4 = WX / 4;
+            const uint4* d4 = reinterpret_cast<const uint4*>(dwin);
+            const float inv = item.inv_scale;
+            for (int i = tid; i < WY * W4 && !abort_flag; i += kBulkConsumers) {
+                const int r = i / W4, c4 = i - r * W4;
+                const int gy = item.y0 + r, gx = item.x0 + 4 * c4;
+                if (gy < 0 || gy >= N || gx < 0 || gx >= N) continue;
+                const uint4 q = d4[i];
+                if ((q.x | q.y | q.z | q.w) != 0u)
+                    red_add_v4(rho + size_t(gy) * N + gx,
+                               make_float4(__uint2float_rn(q.x) * inv, __uint2float_rn(q.y) * inv,
+                                           __uint2float_rn(q.z) * inv, __uint2float_rn(q.w) * inv));
+            }
+            bulk::named_sync(kBulkConsumers);
+        }
+    }
+}
+
 // ---- the fused step kernel, no tile order (global gathers and atomics) -----------------------
 template <int CIC>
 __global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p, int64_t ngroups,
@@ -363,21 +527,35 @@ int work_item_size(int64_t Pq, int nsm) {
 
 size_t max_work_items(int64_t Pq, int ntiles, int item_size) { return size_t(Pq / item_size) + size_t(ntiles) + 1; }
 
+// The fused step kernel in use: particles staged by bulk copies (default), or
+// loaded by each thread (CPM_FUSED_BULK=0).
+#ifndef CPM_FUSED_BULK
+#define CPM_FUSED_BULK 1
+#endif
+size_t fused_tiles_smem(int gran) {
+    return (CPM_FUSED_BULK ? size_t(kBulkStages) * kBulkStageFloats * sizeof(float) : 0) + tile_window_smem(gran);
+}
+constexpr int kFusedLaunchThreads = CPM_FUSED_BULK ? kBulkThreads : kFusedThreads;
+
 template <int CIC, int GRAN>
-static cudaError_t prep_tiles() {
-    return cudaFuncSetAttribute(k_fused_tiles<CIC, GRAN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(tile_window_smem(GRAN)));
+static auto fused_kernel() {
+#if CPM_FUSED_BULK
+    return k_fused_tiles_bulk<CIC, GRAN>;
+#else
+    return k_fused_tiles<CIC, GRAN>;
+#endif
 }
 
 cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid) {
     cudaError_t e = cudaErrorInvalidValue;
     int per_sm = 0;
-    const size_t smem = tile_window_smem(gran);
-#define CPM_TILES(C, G)                                                                                       \
-    if (cic == C && gran == G) {                                                                              \
-        e = prep_tiles<C, G>();                                                                               \
-        if (e == cudaSuccess)                                                                                 \
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tiles<C, G>, kFusedThreads, smem); \
+    const size_t smem = fused_tiles_smem(gran);
+#define CPM_TILES(C, G)                                                                                        \
+    if (cic == C && gran == G) {                                                                               \
+        e = cudaFuncSetAttribute(fused_kernel<C, G>(), cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
+        if (e == cudaSuccess)                                                                                  \
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fused_kernel<C, G>(), kFusedLaunchThreads, \
+                                                              smem);                                           \
     }
     CPM_TILES(0, 4) CPM_TILES(0, 5) CPM_TILES(0, 6) CPM_TILES(1, 4) CPM_TILES(1, 5) CPM_TILES(1, 6)
 #undef CPM_TILES
@@ -411,13 +589,22 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
 
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
-                               cudaStream_t st) {
-    const size_t smem = tile_window_smem(gran);
+                               int* status, cudaStream_t st) {
+    const size_t smem = fused_tiles_smem(gran);
+#if CPM_FUSED_BULK
+#define CPM_TILES(C, G)                                                                                      \
+    if (cic == C && gran == G) {                                                                             \
+        return launch_dependent(N >= kDependentMinN, k_fused_tiles_bulk<C, G>, dim3(grid),                    \
+                                dim3(kBulkThreads), smem, st, items, n_items, p, force, rho, N, dt, status); \
+    }
+#else
+    (void)status;
 #define CPM_TILES(C, G)                                                                                      \
     if (cic == C && gran == G) {                                                                             \
         return launch_dependent(N >= kDependentMinN, k_fused_tiles<C, G>, dim3(grid),                         \
                                 dim3(kFusedThreads), smem, st, items, n_items, p, force, rho, N, dt);        \
     }
+#endif
     CPM_TILES(0, 4) CPM_TILES(0, 5) CPM_TILES(0, 6) CPM_TILES(1, 4) CPM_TILES(1, 5) CPM_TILES(1, 6)
 #undef CPM_TILES
     return cudaErrorInvalidValue;

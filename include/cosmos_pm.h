@@ -237,8 +237,10 @@ int cosmos_pm_diagnostics(cosmos_pm* h, double* kinetic, double* potential, doub
  * benchmarks: times[i] in the order prologue deposit (first step after the
  * state was written, else 0), FFT passes (spectral mode: all force passes),
  * stencil (gradient mode), fused gather + update + deposit, tile sort (0 when
- * the step did not sort).  Profiled steps run as direct launches with events
- * between the stages.  *n = capacity on entry, entries written on return. */
+ * the step did not sort).  A profiled step runs as one step per graph launch
+ * (direct launches when graphs are off) with events recorded between its
+ * stages; the prologue and the sort run before it as direct launches.
+ * *n = capacity on entry, entries written on return. */
 int cosmos_pm_set_profiling(cosmos_pm* h, int32_t enabled);
 int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n);
 

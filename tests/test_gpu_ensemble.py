@@ -133,3 +133,50 @@ def test_ensemble_rejects_bad_configs():
         with pytest.raises(_lib.CosmosError):
             ens.get_particles(0, 9)       # beyond P_0
         assert ens.launches_per_step() == 2 * 6
+
+
+def test_ensemble_members_match_fp64_oracle():
+    """Members of an ensemble at the batched form's lattice sizes (256^2,
+    512^2, 1024^2) against the FP64 oracle on each member's own GPU
+    positions: the fused kernel's deposit <= 1e-6, the force the next step
+    uses (computed from that deposit) <= 1e-5, and the positions after that
+    step within 1e-3 cells of one FP64 oracle step (CosmosCuda.cuh:1209-1300)."""
+    from cosmossimulationwithcuda_gb300 import _lib, ics
+    from oracle import pm_oracle
+    dt = 0.002
+    members = [(256, 40_000, "binary", 31), (512, 400_000, "disk", 32), (1024, 1_200_000, "disk", 33),
+               (512, 60_000, "binary", 34)]
+    states = []
+    for N, P, kind, seed in members:
+        if kind == "binary":
+            states.append(ics.binary_star(P, N, dt, seed=seed))
+        else:
+            states.append(ics.exponential_disk(P, N, dt, seed=seed, scale=N / 10.0))
+    Ns = [m[0] for m in members]
+    Ps = [m[1] for m in members]
+    with _lib.Ensemble(Ns, Ps, cic=True, dt=dt, force_mode=_lib.FORCE_SPECTRAL, sort_interval=8) as ens:
+        for i, st in enumerate(states):
+            ens.set_state(i, st)
+        ens.step(5)
+        ens.synchronize()
+        before = [ens.get_particles(i) for i in range(len(members))]
+        dens = [ens.get_field(i, _lib.FIELD_DENSITY) for i in range(len(members))]
+        ens.step(1)
+        ens.synchronize()
+        after = [ens.get_particles(i) for i in range(len(members))]
+        frc = [ens.get_field(i, _lib.FIELD_FORCE) for i in range(len(members))]
+    pm_oracle.set_threads(pm_oracle.max_threads())
+    for i, (N, P, _, _) in enumerate(members):
+        x, y, xo, yo, m = before[i]
+        o = pm_oracle.OraclePM(N, True, dt, 1.0, fp64=True)
+        o.deposit(x, y, m)
+        assert rel_l2(dens[i], o.density()) <= 1e-6, (i, rel_l2(dens[i], o.density()))
+        o.potential()
+        o.gradient()
+        assert rel_l2(frc[i], o.force()) <= 1e-5, (i, rel_l2(frc[i], o.force()))
+        rx, ry, rxo, ryo = x.copy(), y.copy(), xo.copy(), yo.copy()
+        o.integrate(rx, ry, rxo, ryo)
+        o.close()
+        keep = (x > 3) & (x < N - 3) & (y > 3) & (y < N - 3)
+        assert np.abs(after[i][0] - rx)[keep].max() <= 1e-3, i
+        assert np.abs(after[i][1] - ry)[keep].max() <= 1e-3, i

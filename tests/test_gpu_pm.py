@@ -423,3 +423,31 @@ def test_diagnostics_unwraps_wrapped_particles(cosmos_lib):
     d = (np.float64(x[0]) - np.float64(xo[0])) + (N - 4)
     assert abs(px - d / dt) <= 1e-9 * abs(d / dt) + 1e-12
     assert abs(ke - 0.5 * (d / dt) ** 2) <= 1e-9 * ke
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_stage_times_of_profiled_steps(cosmos_lib, use_graph):
+    """Profiled steps (graph-launched with event nodes between the stages, or
+    direct launches) report positive stage times and advance the state
+    exactly like unprofiled steps (NGP, unit masses: bit-exact)."""
+    N, P, dt = 1024, 1 << 18, 0.002
+    st = ics.uniform(P, N, dt, seed=6)
+    outs = []
+    for profile in (True, False):
+        with _sim(cosmos_lib, N, P, False, dt=dt, sort_interval=4, use_graph=use_graph,
+                  force_mode=cosmos_lib.FORCE_SPECTRAL) as s:
+            s.set_state(st)
+            s.set_profiling(profile)
+            sorts = 0
+            for _ in range(6):
+                s.step(1)
+                if profile:
+                    t = s.stage_times()
+                    assert t[1] > 0 and t[3] > 0  # force passes, fused step
+                    sorts += int(t[4] > 0)
+            s.synchronize()
+            if profile:
+                assert sorts == 2  # steps 1 and 5
+            outs.append(s.get_particles())
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
