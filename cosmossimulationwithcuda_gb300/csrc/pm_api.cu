@@ -74,6 +74,8 @@ struct cosmos_pm {
     void* tc_dft = nullptr;   // tensor-core modes: DFT matrix image
     int* tc_status = nullptr; // tensor-core modes: MMA wait timeout flag
     int* wait_status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
+    cpm::SpectralMaps maps{};    // spectral mode from 256^2 up: tensor maps of the row and column passes' tiles
+    bool have_maps = false;
     cpm::SpectralTc tc{};
     float* kq = nullptr;
     float2* tw = nullptr;
@@ -194,7 +196,8 @@ cudaError_t record_profile_event(cudaEvent_t ev, cudaStream_t st) {
 int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
     CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
                                         h->cfg.gravity_multiplier, st, h->aux_stream, h->fork_ev, h->join_ev, 1,
-                                        is_tc(h->cfg.force_mode) ? &h->tc : nullptr, clear_rho ? h->rho : nullptr));
+                                        is_tc(h->cfg.force_mode) ? &h->tc : nullptr, clear_rho ? h->rho : nullptr,
+                                        h->have_maps ? &h->maps : nullptr, h->wait_status));
     return COSMOS_OK;
 }
 
@@ -592,6 +595,12 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         }
         if (cpm::prepare_spectral_passes(N) != cudaSuccess)
             return bail(cpm::fail(COSMOS_ERR_CUDA, "spectral kernel attributes"));
+        if (N >= 256) {  // tiles of the row and column passes arrive by tensor-map loads
+            const cudaError_t me = cpm::make_spectral_maps(N, h->rho, h->spec, 1, &h->maps);
+            if (me != cudaSuccess)
+                return bail(cpm::fail(COSMOS_ERR_CUDA, std::string("tensor maps: ") + cudaGetErrorString(me)));
+            h->have_maps = true;
+        }
         if (cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess)

@@ -54,6 +54,8 @@ struct EnsClass {
     cpm::RadixScratch rs{};
     uint32_t *tstart = nullptr, *tend = nullptr, *n_items = nullptr;
     int* status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
+    cpm::SpectralMaps maps{};
+    bool have_maps = false;
     cpm::WorkItem* items = nullptr;
     size_t max_items = 0;
     int item_size = cpm::kItemMax;
@@ -193,7 +195,13 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
     CPM_CUDA(cudaMemsetAsync(c.n_items, 0, sizeof(uint32_t), st));
     CPM_CUDA(cudaMemsetAsync(c.status, 0, sizeof(int), st));
     CPM_CUDA(cpm::prepare_conv_passes(c.N));
-    if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) CPM_CUDA(cpm::prepare_spectral_passes(c.N));
+    if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
+        CPM_CUDA(cpm::prepare_spectral_passes(c.N));
+        if (c.N >= 256) {  // the class's lattices as one batch of tensor-map tiles
+            CPM_CUDA(cpm::make_spectral_maps(c.N, c.rho, c.spec, c.nsims, &c.maps));
+            c.have_maps = true;
+        }
+    }
     CPM_CUDA(cpm::prepare_tile_kernels(c.gran, e->cic, e->nsm, &c.tiles_grid));
     CPM_TRY(cpm::build_filter(c.N, e->cic, c.kq, c.tw, st));
     const uint64_t T = uint64_t(c.N >> c.gran);
@@ -307,7 +315,8 @@ int class_body(cosmos_ensemble* e, EnsClass& c) {
     const float g = e->cfg.gravity_multiplier;
     if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
         CPM_CUDA(cpm::launch_spectral_force(c.N, c.rho, c.spec, c.spec2, c.edge, c.dy, c.kq, c.force, c.tw, g, st, c.aux,
-                                            c.fork, c.join, c.nsims));
+                                            c.fork, c.join, c.nsims, nullptr, nullptr,
+                                            c.have_maps ? &c.maps : nullptr, c.status));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(c.N, c.rho, c.spec, c.kq, c.phi, c.tw, st, c.nsims));
         CPM_CUDA(cpm::launch_gradient(c.phi, c.force, c.N, g, st, c.nsims));

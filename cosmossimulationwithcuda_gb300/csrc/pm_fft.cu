@@ -32,6 +32,7 @@
 
 #include "fft_engine.cuh"
 #include "pm_internal.h"
+#include "tma.cuh"
 
 namespace cpm {
 
@@ -108,24 +109,14 @@ struct FitBlocks {
 };
 
 // ---- pass 1: rows, real -> half spectrum, transposed store --------------------------------
-template <class T, int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(cplx_t<T>),
-                                                 MinBlocks<NT>::value, sizeof(T) == 8 ? 128 : 64>::value))
-    k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
-                                                 const cplx_t<T>* __restrict__ tw, T* clear) {
+// Body of the row pass: B rows from `src(line, i)` (row `line` as M complex
+// values z[n] = (x[2n], x[2n+1])), transformed in shared memory `s`.
+template <class T, int N, int B, int NT, class Src>
+__device__ __forceinline__ void r2c_rows(const Src& src, cplx_t<T>* s, cplx_t<T>* __restrict__ spec,
+                                         const cplx_t<T>* __restrict__ tw, T* clear, int y0) {
     using C = cplx_t<T>;
     constexpr int M = N / 2;
     constexpr int LP = LinePad<M>::value;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s = reinterpret_cast<C*>(smem_raw);
-    dependency_wait();
-    allow_dependents();
-    const int y0 = int(blockIdx.x) * B;
-    in += size_t(blockIdx.y) * N * N;
-    spec += size_t(blockIdx.y) * M * N;
-    // Row b as M complex values z[n] = (x[2n], x[2n+1]).
-    const C* rows = reinterpret_cast<const C*>(in + size_t(y0) * N);
-    auto src = [rows](int line, int i) { return rows[line * M + i]; };
     auto dst = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
     fft_lines<M, B, NT, -1, C, kMaxRadix>(s, src, dst, tw, 2);
     if (clear) {  // the rows were read (fft_lines ends with a barrier): zero them for the next deposit
@@ -148,6 +139,85 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>:
         }
         spec[size_t(k) * N + y0 + b] = out;
     }
+}
+
+template <class T, int N, int B, int NT>
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(cplx_t<T>),
+                                                 MinBlocks<NT>::value, sizeof(T) == 8 ? 128 : 64>::value))
+    k_rows_r2c(const T* __restrict__ in, cplx_t<T>* __restrict__ spec,
+                                                 const cplx_t<T>* __restrict__ tw, T* clear) {
+    using C = cplx_t<T>;
+    constexpr int M = N / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    dependency_wait();
+    allow_dependents();
+    const int y0 = int(blockIdx.x) * B;
+    in += size_t(blockIdx.y) * N * N;
+    spec += size_t(blockIdx.y) * M * N;
+    const C* rows = reinterpret_cast<const C*>(in + size_t(y0) * N);
+    auto src = [rows](int line, int i) { return rows[line * M + i]; };
+    r2c_rows<T, N, B, NT>(src, s, spec, tw, clear, y0);
+}
+
+// The dynamic shared memory of a kernel is only guaranteed 16-byte alignment;
+// a tensor-map load needs a 128-byte aligned destination.  TMA kernels ask for
+// kTmaAlignPad extra bytes and start their tiles at the next 128-byte boundary.
+constexpr size_t kTmaAlignPad = 128;
+__device__ __forceinline__ unsigned char* align128(unsigned char* p) {
+    const uint32_t a = bulk::smem_u32(p);
+    return p + ((128u - (a & 127u)) & 127u);
+}
+
+// Self-check before a tensor-map load: a destination off the 128-byte grid is
+// recorded (*status = 3) and the tile skipped, never handed to the copy engine
+// (the same answer in every thread of the CTA).
+__device__ __forceinline__ bool tma_dst_ok(const void* dst, int* status) {
+    if ((bulk::smem_u32(dst) & 127u) == 0u) return true;
+    if (threadIdx.x == 0) atomicMax(status, 3);
+    return false;
+}
+
+// A bounded TMA wait, decided for the whole CTA: false (every thread) when any
+// thread's wait ran out; thread 0 then records it and waits once more for the
+// copy in flight, so that it has landed before the CTA releases its shared memory.
+__device__ __forceinline__ bool tile_landed(bool ok, uint64_t* bar, int* status) {
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0) atomicMax(status, bulk::wait(bar, 0) ? 1 : 2);
+    return ok;
+}
+
+// The row pass with its B rows staged by one tensor-map load (TMA) into the
+// same shared memory the transform then works in: the first radix stage reads
+// every input value into registers before it stores (fft_stage), so the dense
+// tile and the padded lines can share the space.
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N / 2>::value * sizeof(float2),
+                                                 MinBlocks<NT>::value, 64>::value))
+    k_rows_r2c_tma(const __grid_constant__ CUtensorMap rho_map, float2* __restrict__ spec,
+                   const float2* __restrict__ tw, float* clear, int* status) {
+    using C = float2;
+    constexpr int M = N / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    C* s = reinterpret_cast<C*>(align128(smem_raw));
+    if (threadIdx.x == 0) {
+        bulk::mbar_init(&bar, 1);
+        bulk::fence_barrier_init();
+        tma::prefetch_map(&rho_map);
+    }
+    __syncthreads();
+    dependency_wait();
+    allow_dependents();
+    const int y0 = int(blockIdx.x) * B;
+    if (!tma_dst_ok(s, status)) return;
+    if (!tile_landed(tma::load_rows_sync(s, &rho_map, y0, int(blockIdx.y), uint32_t(B) * N * 4u, &bar, 0), &bar,
+                     status))
+        return;
+    spec += size_t(blockIdx.y) * M * N;
+    const C* land = s;
+    auto src = [land](int line, int i) { return land[line * M + i]; };
+    r2c_rows<float, N, B, NT>(src, s, spec, tw, clear, y0);
 }
 
 // ---- pass 2: columns, forward FFT x K x inverse FFT ----------------------------------------
@@ -336,28 +406,18 @@ __device__ __forceinline__ void block_sum(float (&v)[K], float* red) {
 // y: Phi = IFFT_y(phi_hat) (back into spec) and Psi = IFFT_y(phi_hat * i S(ky) * g)
 // (into spec2); and the three y-edge differences of every line,
 // edge[kx * 4 + j] = sum_ky phi_hat(kx, ky) w_j(ky).
-template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>::value * sizeof(float2),
-                                                 CPM_COLS_SPECTRAL_MINB, (N <= CPM_COLS_FULL_MAX_N ? 64 : 128)>::value))
-    k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
-                                                         float2* __restrict__ edge, const float* __restrict__ kq,
-                                                         const float2* __restrict__ tw, float g) {
+// Body for B lines from `src(line, i)`; `lines` / `lines2` receive Phi / Psi.
+template <int N, int B, int NT, class Src>
+__device__ __forceinline__ void cols_spectral_lines(const Src& src, float2* s, float2* __restrict__ lines,
+                                                    float2* __restrict__ lines2, float2* __restrict__ edge,
+                                                    const float* __restrict__ kq, const float2* __restrict__ tw,
+                                                    float g, int kx0) {
     using C = float2;
     constexpr int M = N / 2;
     constexpr int LP = LinePad<N>::value;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): phi_hat; [B, 2B): phi_hat * iS
     float* red = reinterpret_cast<float*>(s + 2 * B * LP);
-    dependency_wait();
-    allow_dependents();
-    const int kx0 = int(blockIdx.x) * B;
-    spec += size_t(blockIdx.y) * M * N;
-    spec2 += size_t(blockIdx.y) * M * N;
-    edge += size_t(blockIdx.y) * M * 4;
-    C* lines = spec + size_t(kx0) * N;
-    auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
     auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<N, B, NT, -1, C, kMaxRadix>(s, gload, sstore, tw, 1);
+    fft_lines<N, B, NT, -1, C, kMaxRadix>(s, src, sstore, tw, 1);
     for (int idx = threadIdx.x; idx < B * (M + 1); idx += NT) {
         const int b = idx / (M + 1);
         const int ky = idx - b * (M + 1);
@@ -399,7 +459,6 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
         }
     }
     __syncthreads();
-    C* lines2 = spec2 + size_t(kx0) * N;
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto gstore2 = [lines, lines2](int line, int i, C v) {
         if (line < B)
@@ -408,6 +467,71 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
             lines2[size_t(line - B) * N + i] = v;
     };
     fft_lines<N, 2 * B, NT, +1, C, kMaxRadix>(s, sload, gstore2, tw, 1);
+}
+
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>::value * sizeof(float2),
+                                                 CPM_COLS_SPECTRAL_MINB, (N <= CPM_COLS_FULL_MAX_N ? 64 : 128)>::value))
+    k_cols_spectral(float2* __restrict__ spec, float2* __restrict__ spec2,
+                                                         float2* __restrict__ edge, const float* __restrict__ kq,
+                                                         const float2* __restrict__ tw, float g) {
+    using C = float2;
+    constexpr int M = N / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);  // lines [0, B): phi_hat; [B, 2B): phi_hat * iS
+    dependency_wait();
+    allow_dependents();
+    const int kx0 = int(blockIdx.x) * B;
+    spec += size_t(blockIdx.y) * M * N;
+    spec2 += size_t(blockIdx.y) * M * N;
+    edge += size_t(blockIdx.y) * M * 4;
+    C* lines = spec + size_t(kx0) * N;
+    auto gload = [lines](int line, int i) { return lines[size_t(line) * N + i]; };
+    cols_spectral_lines<N, B, NT>(gload, s, lines, spec2 + size_t(kx0) * N, edge, kq, tw, g, kx0);
+}
+
+// Byte offset (from the 128-byte aligned base) of the TMA landing tile of the
+// spectral column pass: the B dense lines land in the upper half of the shared
+// lines (phi_hat * iS, unused until after the forward transform), on a
+// 128-byte boundary.
+template <int N, int B>
+constexpr size_t cols_land_offset() {
+    return ((2 * size_t(B) * LinePad<N>::value - size_t(B) * N) * sizeof(float2)) & ~size_t(127);
+}
+
+// The spectral column pass with its B lines staged by one tensor-map load.
+template <int N, int B, int NT>
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>::value * sizeof(float2),
+                                                 CPM_COLS_SPECTRAL_MINB, (N <= CPM_COLS_FULL_MAX_N ? 64 : 128)>::value))
+    k_cols_spectral_tma(const __grid_constant__ CUtensorMap spec_map, float2* __restrict__ spec,
+                        float2* __restrict__ spec2, float2* __restrict__ edge, const float* __restrict__ kq,
+                        const float2* __restrict__ tw, float g, int* status) {
+    using C = float2;
+    constexpr int M = N / 2;
+    static_assert(cols_land_offset<N, B>() >= size_t(B) * LinePad<N>::value * sizeof(float2), "landing tile");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    unsigned char* base = align128(smem_raw);
+    C* s = reinterpret_cast<C*>(base);
+    C* land = reinterpret_cast<C*>(base + cols_land_offset<N, B>());
+    if (threadIdx.x == 0) {
+        bulk::mbar_init(&bar, 1);
+        bulk::fence_barrier_init();
+        tma::prefetch_map(&spec_map);
+    }
+    __syncthreads();
+    dependency_wait();
+    allow_dependents();
+    const int kx0 = int(blockIdx.x) * B;
+    if (!tma_dst_ok(land, status)) return;
+    if (!tile_landed(tma::load_rows_sync(land, &spec_map, kx0, int(blockIdx.y), uint32_t(B) * N * 8u, &bar, 0),
+                     &bar, status))
+        return;
+    spec += size_t(blockIdx.y) * M * N;
+    spec2 += size_t(blockIdx.y) * M * N;
+    edge += size_t(blockIdx.y) * M * 4;
+    auto lload = [land](int line, int i) { return land[line * N + i]; };
+    cols_spectral_lines<N, B, NT>(lload, s, spec + size_t(kx0) * N, spec2 + size_t(kx0) * N, edge, kq, tw, g, kx0);
 }
 
 // Rows, spectral force: C2R of Fx = IFFT_x(i S(kx) g Phi) and Fy = IFFT_x(Psi)
@@ -606,20 +730,53 @@ struct SpecShape {
 // The 3-row C2R of the y-edge differences only feeds the 4 boundary rows: it
 // runs on the auxiliary stream, concurrent with the main C2R pass (fork/join
 // with events, which CUDA-graph capture records as graph edges).
+// The tensor-map (TMA) variants of the row and column passes serve lattices
+// from kTmaMinN up (smaller lattices keep per-thread loads: their tiles are a
+// few KB and their landing space would not fit beside the padded lines).
+constexpr int kTmaMinN = 256;
+// CPM_SPECTRAL_TMA=0 builds the per-thread-load passes only (for comparisons).
+#ifndef CPM_SPECTRAL_TMA
+#define CPM_SPECTRAL_TMA 1
+#endif
+
 template <int N>
 static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                      const float* kq, float2* force, const float2* tw, float g, int batch,
                                      cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join,
-                                     const SpectralTc* tc, float* clear) {
+                                     const SpectralTc* tc, float* clear, const SpectralMaps* maps, int* status) {
     using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
     const bool dependent = N >= kDependentMinN;
-    cudaError_t e;
-    if ((e = launch_dependent(dependent, k_rows_r2c<float, N, RS::B, RS::NT>, dim3(N / RS::B, batch), dim3(RS::NT),
+    const bool tma = CPM_SPECTRAL_TMA && N >= kTmaMinN && maps != nullptr && status != nullptr;
+    cudaError_t e = cudaSuccess;
+    bool cols_done = false;
+    if constexpr (N >= kTmaMinN) {
+        if (tma) {
+            if ((e = launch_dependent(dependent, k_rows_r2c_tma<N, RS::B, RS::NT>, dim3(N / RS::B, batch),
+                                      dim3(RS::NT), RS::smem + kTmaAlignPad, st, maps->rho, spec, tw, clear,
+                                      status)) != cudaSuccess)
+                return e;
+            if (!tc) {
+                if (batch == 1 && SS::CNT != CS::NT)
+                    e = launch_dependent(dependent, k_cols_spectral_tma<N, CS::B, SS::CNT>, dim3(N / 2 / CS::B),
+                                         dim3(SS::CNT), SS::col_smem_for(SS::CNT) + kTmaAlignPad, st, maps->spec,
+                                         spec, spec2, edge, kq, tw, g, status);
+                else
+                    e = launch_dependent(dependent, k_cols_spectral_tma<N, CS::B, CS::NT>,
+                                         dim3((N / 2) / CS::B, batch), dim3(CS::NT), SS::col_smem + kTmaAlignPad, st,
+                                         maps->spec, spec, spec2, edge, kq, tw, g, status);
+                if (e != cudaSuccess) return e;
+                cols_done = true;
+            }
+        }
+    }
+    if (!tma &&
+        (e = launch_dependent(dependent, k_rows_r2c<float, N, RS::B, RS::NT>, dim3(N / RS::B, batch), dim3(RS::NT),
                               RS::smem, st, rho, spec, tw, clear)) != cudaSuccess)
         return e;
-    if (tc) {
+    if (cols_done) {
+    } else if (tc) {
         if ((e = launch_cols_spectral_tc(N, tc->bf16, spec, spec2, edge, kq, tw, tc->dft, g, tc->status,
                                          tc->skip_mma, batch, st)) != cudaSuccess)
             return e;
@@ -646,9 +803,18 @@ static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spe
 
 template <int N>
 static cudaError_t prepare_spectral_n() {
+    using RS = RowShape<float, N>;
     using CS = ColShape<float, N>;
     using SS = SpecShape<N>;
     cudaError_t e;
+    if constexpr (N >= kTmaMinN) {
+        if ((e = allow_smem(k_rows_r2c_tma<N, RS::B, RS::NT>, RS::smem + kTmaAlignPad)) != cudaSuccess) return e;
+        if ((e = allow_smem(k_cols_spectral_tma<N, CS::B, CS::NT>, SS::col_smem + kTmaAlignPad)) != cudaSuccess)
+            return e;
+        if ((e = allow_smem(k_cols_spectral_tma<N, CS::B, SS::CNT>, SS::col_smem_for(SS::CNT) + kTmaAlignPad)) !=
+            cudaSuccess)
+            return e;
+    }
     if ((e = allow_smem(k_cols_spectral<N, CS::B, CS::NT>, SS::col_smem)) != cudaSuccess) return e;
     if ((e = allow_smem(k_cols_spectral<N, CS::B, SS::CNT>, SS::col_smem_for(SS::CNT))) != cudaSuccess) return e;
     if ((e = allow_smem(k_rows_c2r<N, 1, SS::ENT, 4>, SS::edge_smem)) != cudaSuccess) return e;
@@ -667,17 +833,42 @@ cudaError_t prepare_spectral_passes(int N) {
     }
 }
 
+template <int N>
+static cudaError_t spectral_maps_n(const float* rho, const float2* spec, int batch, SpectralMaps* maps) {
+    if constexpr (N < kTmaMinN) {
+        return cudaErrorNotSupported;
+    } else {
+        using RS = RowShape<float, N>;
+        using CS = ColShape<float, N>;
+        cudaError_t e = make_row_map(&maps->rho, rho, N, N, batch, RS::B);
+        if (e == cudaSuccess) e = make_row_map(&maps->spec, spec, 2 * N, N / 2, batch, CS::B);
+        return e;
+    }
+}
+
+cudaError_t make_spectral_maps(int N, const float* rho, const float2* spec, int batch, SpectralMaps* maps) {
+    switch (N) {
+#define CPM_CASE(n) \
+    case n:         \
+        return spectral_maps_n<n>(rho, spec, batch, maps);
+        CPM_FOR_EACH_N(CPM_CASE)
+#undef CPM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
                                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch,
-                                  const SpectralTc* tc, float* clear) {
+                                  const SpectralTc* tc, float* clear, const SpectralMaps* maps, int* status) {
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
     if (tc && !tc_fft_supported(N)) return cudaErrorInvalidValue;
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
         return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join, tc, \
-                                    clear);
+                                    clear, maps, status);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:

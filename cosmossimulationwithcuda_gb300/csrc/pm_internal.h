@@ -1,6 +1,7 @@
 // Host-side launchers shared between the translation units of cosmos_pm.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -32,14 +33,29 @@ cudaError_t prepare_tc_columns(int N, int bf16, void* dft_dev, cudaStream_t st);
 cudaError_t launch_cols_spectral_tc(int N, int bf16, float2* spec, float2* spec2, float2* edge, const float* kq,
                                     const float2* tw, const void* dft_dev, float g, int* status, int skip_mma,
                                     int batch, cudaStream_t st);
+// pm_tma.cu: a row map (tma.cuh) of `rows` rows of `rowlen` floats for each
+// of `batch` lattices stored back to back, loaded in boxes of `box_rows` rows.
+cudaError_t make_row_map(CUtensorMap* map, const void* base, int rowlen, int rows, int batch, int box_rows);
+// The row maps the spectral force's row and column passes load their tiles
+// through: the density (rows of N floats) and the half spectrum's column lines
+// (lines of N complex).  make_spectral_maps: cudaErrorNotSupported below
+// 256^2 (those lattices keep per-thread loads).
+struct SpectralMaps {
+    CUtensorMap rho;
+    CUtensorMap spec;
+};
+cudaError_t make_spectral_maps(int N, const float* rho, const float2* spec, int batch, SpectralMaps* maps);
 // Test hook of the device allocations: true when this allocation must fail.
 bool alloc_should_fail();
 // aux/fork/join: an auxiliary stream and two events for the concurrent edge pass;
-// tc: the tensor-core column pass instead of the FP32 one (nullptr: FP32).
+// tc: the tensor-core column pass instead of the FP32 one (nullptr: FP32);
+// maps + status: the row and column passes load their tiles through the
+// tensor maps (from 256^2 up), and a load wait that runs out sets *status.
 cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
                                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1,
-                                  const SpectralTc* tc = nullptr, float* clear = nullptr);
+                                  const SpectralTc* tc = nullptr, float* clear = nullptr,
+                                  const SpectralMaps* maps = nullptr, int* status = nullptr);
 int spectral_launches_per_step();
 
 // pm_particles.cu
