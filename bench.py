@@ -303,8 +303,10 @@ IC_TEXT = {
 
 
 def run_ensemble(args, ws, rank, local):
-    """The 64-simulation ensemble: device-timed steps of all simulations (one
-    graph launch per step), particle-steps/s summed over the simulations."""
+    """The 64-simulation ensemble: device-timed steps of all simulations,
+    particle-steps/s summed over the simulations.  Both forms of the step are
+    timed (one graph of per-pass kernels per step; one persistent cooperative
+    launch per step) and the faster one is reported, the other beside it."""
     from cosmossimulationwithcuda_gb300 import _build, _lib, ics
     e = ics.ENSEMBLE
     Ns, Ps, states = ics.ensemble_workload()
@@ -314,25 +316,40 @@ def run_ensemble(args, ws, rank, local):
     rt.lib.cudaSetDevice(local)
     mode = {"spectral": _lib.FORCE_SPECTRAL, "gradient": _lib.FORCE_GRADIENT, "tc-fp16": _lib.FORCE_SPECTRAL_TC_FP16,
             "tc-bf16": _lib.FORCE_SPECTRAL_TC_BF16}[args.force_mode]
-    ens = _lib.Ensemble(Ns, Ps, cic=e["cic"], dt=e["dt"], device=local, force_mode=mode,
-                        sort_interval=args.sort_interval if args.sort_interval > 0 else 32)
-    for i, st in enumerate(states):
-        ens.set_state(i, st)
-    stream = ens.stream()
+    def timed_form(persistent: bool):
+        """Device-timed steps of one form of the ensemble step: one graph of
+        per-pass kernels per step, or one persistent cooperative launch."""
+        ens = _lib.Ensemble(Ns, Ps, cic=e["cic"], dt=e["dt"], device=local, force_mode=mode,
+                            sort_interval=args.sort_interval if args.sort_interval > 0 else 32, persistent=persistent)
+        for i, st in enumerate(states):
+            ens.set_state(i, st)
+        ens.step(args.warmup)
+        ens.synchronize()
+        barrier(ws)
+        win = timed_windows(rt, ens.stream(), ens.step, steps, min_ms=args.min_timed_ms)
+        ens.synchronize()
+        per = ens.launches_per_step()
+        return ens, max_over_ranks(sum(win) / (steps * len(win)), ws), steps * len(win), per
+
     steps = args.steps
+    forms = {}
+    persistent_ok = mode == _lib.FORCE_SPECTRAL and all(128 <= n <= 1024 for n in Ns)
     clk = ClockSampler(local).__enter__()
-    ens.step(args.warmup)
-    ens.synchronize()
     clk.wait_first()
-    barrier(ws)
     try:
-        windows = timed_windows(rt, stream, ens.step, steps, min_ms=args.min_timed_ms)
+        for persistent in ((False, True) if persistent_ok else (False,)):
+            ens_f, ms_f, tsteps_f, per_f = timed_form(persistent)
+            forms["persistent" if persistent else "graph"] = (ens_f, ms_f, tsteps_f, per_f)
     finally:
         clk.__exit__()
-    ens.synchronize()
-    timed_steps = steps * len(windows)
-    ms_step = max_over_ranks(sum(windows) / timed_steps, ws)
-    launches = ens.launches_per_step() * timed_steps
+    best = min(forms, key=lambda k: forms[k][1])
+    for k, v in forms.items():
+        if k != best:
+            v[0].close()
+    ens, ms_step, timed_steps, per_step = forms[best]
+    launches = per_step * timed_steps
+    form_times = {k: {"ms_per_step": v[1], "launches_per_step": v[3], "value": Ptot / (v[1] / 1e3)}
+                  for k, v in forms.items()}
     # whole-step algorithmic bytes: fused step 36 B/particle + 12 B/cell, density clear (memset) 4 B/cell;
     # force passes 37 B/cell (spectral:
     # FFT passes; gradient: 25 B/cell of FFT passes + 12 B/cell of stencil)
@@ -380,7 +397,7 @@ def run_ensemble(args, ws, rank, local):
             "e2e": {"value": Ptot * e2e_steps / (t1 - t0), "unit": UNIT,
                     "h2d_bytes_per_step": int(20 * Ptot / e2e_steps), "d2h_bytes_per_step": int(20 * Ptot / e2e_steps),
                     "note": f"all states uploaded from page-locked memory, {e2e_steps} steps, all particles read back"},
-            "clocks": clk.summary(), "gpu_launches": launches}
+            "clocks": clk.summary(), "gpu_launches": launches, "step_forms": form_times, "step_form": best}
     print(json.dumps(line), flush=True)
 
 
@@ -431,7 +448,8 @@ def main():
     ap.add_argument("--render-interval", type=int, default=2,
                     help="e2e: read the positions back every this many steps")
     ap.add_argument("--autotune", action="store_true",
-                    help="pick the sort granularity / cadence with cosmos_pm_autotune on this state first")
+                    help="pick the launch shapes (sort tile edge and cadence, work-item size, fused-kernel CTAs "
+                         "per SM, column-pass shape) with cosmos_pm_autotune on this state first")
     ap.add_argument("--no-tc-compare", action="store_true",
                     help="skip the tensor-core split-FFT comparison run of the headline metric")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end runs through host buffers")
@@ -505,19 +523,19 @@ def main():
     rt.lib.cudaSetDevice(local)
     mode = {"spectral": _lib.FORCE_SPECTRAL, "gradient": _lib.FORCE_GRADIENT, "tc-fp16": _lib.FORCE_SPECTRAL_TC_FP16,
             "tc-bf16": _lib.FORCE_SPECTRAL_TC_BF16}[args.force_mode]
-    sort_interval, sort_gran = args.sort_interval, -1
+    shape = {"sort_interval": args.sort_interval, "sort_granularity": -1}
     if args.autotune:
         cache = os.environ.get("COSMOS_PM_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "cosmos_pm",
                                                                      "autotune.txt"))
         os.makedirs(os.path.dirname(cache), exist_ok=True)
         t0 = time.perf_counter()
-        g, itv, tms = _lib.autotune(state, N, cic=cic, dt=dt, device=local, force_mode=mode, steps=128,
+        chosen, tms = _lib.autotune(state, N, cic=cic, dt=dt, device=local, force_mode=mode, steps=128,
                                     cache_path=cache)
-        sort_interval, sort_gran = itv, (g if itv else -1)
-        config["autotune"] = {"sort_granularity": g, "sort_interval": itv, "ms_per_step": tms,
-                              "search_s": round(time.perf_counter() - t0, 2), "cache": cache}
-    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=sort_interval, force_mode=mode,
-                          sort_granularity=sort_gran)
+        shape = dict(chosen)
+        if not shape["sort_interval"]:
+            shape["sort_granularity"] = -1
+        config["autotune"] = dict(chosen, ms_per_step=tms, search_s=round(time.perf_counter() - t0, 2), cache=cache)
+    sim = _lib.Simulation(N, P, cic=cic, dt=dt, device=local, force_mode=mode, **shape)
     stream = sim.stream()
     sim.set_state(state)
     config["force_mode"] = args.force_mode
@@ -676,8 +694,7 @@ def main():
     # FP16 hi/lo split (tc_split_fft) and BF16 hi/lo split (tc_split_fft_bf16)
     def tc_run(force_mode, precision):
         try:
-            with _lib.Simulation(N, P, cic=cic, dt=dt, device=local, sort_interval=sort_interval,
-                                 sort_granularity=sort_gran, force_mode=force_mode) as ts:
+            with _lib.Simulation(N, P, cic=cic, dt=dt, device=local, force_mode=force_mode, **shape) as ts:
                 ts.set_state(state)
                 ts.step(args.warmup)
                 ts.synchronize()

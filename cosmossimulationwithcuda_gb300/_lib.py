@@ -20,7 +20,7 @@ DEPOSIT_NGP, DEPOSIT_CIC = 0, 1
 FORCE_GRADIENT, FORCE_SPECTRAL, FORCE_SPECTRAL_TC_FP16, FORCE_SPECTRAL_TC_BF16 = 0, 1, 2, 3
 FIELD_DENSITY, FIELD_POTENTIAL, FIELD_FORCE = 0, 1, 2
 STAGE_DEPOSIT, STAGE_POTENTIAL, STAGE_FORCE, STAGE_INTEGRATE = 0, 1, 2, 3
-TEST_FAIL_ALLOC, TEST_TC_SKIP_MMA = 1, 2
+TEST_FAIL_ALLOC, TEST_TC_SKIP_MMA, TEST_COPY_WAIT = 1, 2, 3
 
 # Every function include/cosmos_pm.h declares (checked by the CPU test suite).
 EXPORTS = (
@@ -36,7 +36,7 @@ EXPORTS = (
     "cosmos_ensemble_default_config", "cosmos_ensemble_create", "cosmos_ensemble_destroy",
     "cosmos_ensemble_set_particles", "cosmos_ensemble_get_particles", "cosmos_ensemble_step",
     "cosmos_ensemble_synchronize", "cosmos_ensemble_get_field", "cosmos_ensemble_launches_per_step",
-    "cosmos_ensemble_stream", "cosmos_ensemble_last_error",
+    "cosmos_ensemble_stream", "cosmos_ensemble_last_error", "cosmos_ensemble_test_barrier",
 )
 NOALLOC_MAX_PARTICLES = 1 << 20
 
@@ -54,7 +54,10 @@ class Config(ctypes.Structure):
         ("sort_granularity", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
         ("blur_r", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("item_size", ctypes.c_int32),
+        ("fused_ctas_per_sm", ctypes.c_int32),
+        ("fft_shape", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 
@@ -93,7 +96,8 @@ class EnsembleConfig(ctypes.Structure):
         ("force_mode", ctypes.c_int32),
         ("sort_interval", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 8),
+        ("persistent_step", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
     ]
 
 
@@ -169,6 +173,7 @@ def load(path: str | None = None):
         "cosmos_ensemble_launches_per_step": (ctypes.c_int, [_vp, ctypes.POINTER(i32)]),
         "cosmos_ensemble_stream": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint64)]),
         "cosmos_ensemble_last_error": (ctypes.c_char_p, [_vp]),
+        "cosmos_ensemble_test_barrier": (ctypes.c_int, [_vp, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -194,8 +199,9 @@ def default_config(**kw) -> Config:
 
 def autotune(state, N: int, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0, device: int = 0,
              force_mode: int = FORCE_SPECTRAL, steps: int = 128, cache_path: str | None = None):
-    """Fastest (sort_granularity, sort_interval) for this state, measured on the
-    device (cosmos_pm_autotune).  Returns (granularity, interval, ms_per_step)."""
+    """Fastest launch shapes for this state, measured on the device
+    (cosmos_pm_autotune).  Returns ({sort_granularity, sort_interval,
+    item_size, fused_ctas_per_sm, fft_shape}, ms_per_step)."""
     L = load()
     arrs = [np.ascontiguousarray(a, np.float32) for a in (state.x, state.y, state.x_old, state.y_old, state.m)]
     base = default_config(lattice_n=N, deposit=DEPOSIT_CIC if cic else DEPOSIT_NGP, dt=dt,
@@ -207,7 +213,8 @@ def autotune(state, N: int, cic: bool = True, dt: float = 1e-3, gravity_multipli
                               cache_path.encode() if cache_path else None, ctypes.byref(best), ctypes.byref(ms))
     if rc != COSMOS_OK:
         raise CosmosError(rc, L.cosmos_pm_last_error(None).decode())
-    return best.sort_granularity, best.sort_interval, ms.value
+    fields = ("sort_granularity", "sort_interval", "item_size", "fused_ctas_per_sm", "fft_shape")
+    return {f: int(getattr(best, f)) for f in fields}, ms.value
 
 
 class Simulation:
@@ -219,12 +226,14 @@ class Simulation:
 
     def __init__(self, N: int, P: int, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0,
                  device: int = 0, force_mode: int = FORCE_GRADIENT, sort_interval: int = -1,
-                 sort_granularity: int = -1, use_graph: bool = True, blur_r: int = 3):
+                 sort_granularity: int = -1, use_graph: bool = True, blur_r: int = 3, item_size: int = 0,
+                 fused_ctas_per_sm: int = 0, fft_shape: int = 0):
         self.L = load()
         self.cfg = default_config(lattice_n=N, deposit=DEPOSIT_CIC if cic else DEPOSIT_NGP, dt=dt,
                                   gravity_multiplier=gravity_multiplier, num_particles=P, device=device,
                                   force_mode=force_mode, sort_interval=sort_interval,
-                                  sort_granularity=sort_granularity, use_graph=int(use_graph), blur_r=blur_r)
+                                  sort_granularity=sort_granularity, use_graph=int(use_graph), blur_r=blur_r,
+                                  item_size=item_size, fused_ctas_per_sm=fused_ctas_per_sm, fft_shape=fft_shape)
         h = _vp()
         rc = self.L.cosmos_pm_create(ctypes.byref(self.cfg), ctypes.byref(h))
         if rc != COSMOS_OK:
@@ -392,7 +401,8 @@ class Ensemble:
     dt, deposit, gravity multiplier and force mode for all."""
 
     def __init__(self, lattice_n, num_particles, cic: bool = True, dt: float = 1e-3, gravity_multiplier: float = 1.0,
-                 device: int = 0, force_mode: int = FORCE_SPECTRAL, sort_interval: int = 32, use_graph: bool = True):
+                 device: int = 0, force_mode: int = FORCE_SPECTRAL, sort_interval: int = 32, use_graph: bool = True,
+                 persistent: bool = False):
         self.L = load()
         ns = np.ascontiguousarray(lattice_n, np.int32)
         ps = np.ascontiguousarray(num_particles, np.int64)
@@ -408,6 +418,7 @@ class Ensemble:
         cfg.force_mode = force_mode
         cfg.sort_interval = sort_interval
         cfg.use_graph = int(use_graph)
+        cfg.persistent_step = int(persistent)
         self.cfg = cfg
         h = _vp()
         rc = self.L.cosmos_ensemble_create(ctypes.byref(cfg), ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
@@ -463,6 +474,10 @@ class Ensemble:
         out = np.empty((N, N, 2) if field == FIELD_FORCE else (N, N), np.float32)
         self._check(self.L.cosmos_ensemble_get_field(self.h, sim, field, _ptr(out)))
         return out
+
+    def test_barrier(self, value: int):
+        """Test hook of the persistent step: one CTA skips its first grid-barrier arrival."""
+        self._check(self.L.cosmos_ensemble_test_barrier(self.h, value))
 
     def launches_per_step(self) -> int:
         n = ctypes.c_int32()

@@ -74,6 +74,7 @@ struct cosmos_pm {
     void* tc_dft = nullptr;   // tensor-core modes: DFT matrix image
     int* tc_status = nullptr; // tensor-core modes: MMA wait timeout flag
     int* wait_status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
+    uint32_t copy_tx_extra = 0;  // test hook COSMOS_TEST_COPY_WAIT
     cpm::SpectralMaps maps{};    // spectral mode from 256^2 up: tensor maps of the row and column passes' tiles
     bool have_maps = false;
     cpm::SpectralTc tc{};
@@ -197,7 +198,7 @@ int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
     CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
                                         h->cfg.gravity_multiplier, st, h->aux_stream, h->fork_ev, h->join_ev, 1,
                                         is_tc(h->cfg.force_mode) ? &h->tc : nullptr, clear_rho ? h->rho : nullptr,
-                                        h->have_maps ? &h->maps : nullptr, h->wait_status));
+                                        h->have_maps ? &h->maps : nullptr, h->wait_status, h->cfg.fft_shape));
     return COSMOS_OK;
 }
 
@@ -246,7 +247,7 @@ int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     CPM_TRY(rec(kEvFused));
     if (h->items_valid)
         CPM_CUDA(cpm::launch_fused_tiles(h->items, h->n_items, p, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->gran,
-                                         h->tiles_grid, h->wait_status, st));
+                                         h->tiles_grid, h->wait_status, st, h->copy_tx_extra));
     else
         CPM_CUDA(cpm::launch_fused_global(p, h->P, h->force, h->rho, h->N, h->cic, h->cfg.dt, h->nsm, st));
     CPM_TRY(rec(kEvEnd));
@@ -490,6 +491,11 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return cpm::fail(COSMOS_ERR_INVALID, "sort_granularity must be -1 (default) or 4..6 with 2^g <= N");
     if (cfg->blur_r != 0 && (cfg->blur_r < 1 || cfg->blur_r > 15 || cfg->blur_r % 2 == 0))
         return cpm::fail(COSMOS_ERR_INVALID, "blur_r must be 0 (default 3) or odd in [1, 15]");
+    if (cfg->item_size != 0 && cfg->item_size != 2048 && cfg->item_size != 4096 && cfg->item_size != 8192)
+        return cpm::fail(COSMOS_ERR_INVALID, "item_size must be 0 (default), 2048, 4096 or 8192");
+    if (cfg->fused_ctas_per_sm < 0 || cfg->fused_ctas_per_sm > 32)
+        return cpm::fail(COSMOS_ERR_INVALID, "fused_ctas_per_sm must be in [0, 32]");
+    if (cfg->fft_shape != 0 && cfg->fft_shape != 1) return cpm::fail(COSMOS_ERR_INVALID, "fft_shape must be 0 or 1");
     int ndev = 0;
     CPM_CUDA(cudaGetDeviceCount(&ndev));
     if (cfg->device < 0 || cfg->device >= ndev) return cpm::fail(COSMOS_ERR_INVALID, "device ordinal out of range");
@@ -551,7 +557,7 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
             ;
     }
     const int ntiles = (N >> h->gran) * (N >> h->gran);
-    h->item_size = cpm::work_item_size(h->Pq, h->nsm);
+    h->item_size = cfg->item_size ? cfg->item_size : cpm::work_item_size(h->Pq, h->nsm);
     h->max_items = cpm::max_work_items(h->Pq, ntiles, h->item_size);
     if (rc == COSMOS_OK) {
         const size_t nranges = cpm::tile_range_elems(N, h->gran, 1);
@@ -566,6 +572,8 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return bail(cpm::fail(COSMOS_ERR_CUDA, "memset"));
     if (cpm::prepare_tile_kernels(h->gran, h->cic, h->nsm, &h->tiles_grid) != cudaSuccess)
         return bail(cpm::fail(COSMOS_ERR_CUDA, "tile kernel attributes"));
+    if (cfg->fused_ctas_per_sm > 0 && h->tiles_grid > h->nsm * cfg->fused_ctas_per_sm)
+        h->tiles_grid = h->nsm * cfg->fused_ctas_per_sm;
     // zero state; identities; filter
     for (int b = 0; b < 2; ++b) {
         ParticleArrays& a = h->buf[b];
@@ -1276,12 +1284,17 @@ int cosmos_pm_test_hook(cosmos_pm* h, int32_t hook, int64_t value) {
         case COSMOS_TEST_FAIL_ALLOC:
             cpm::g_fail_alloc_countdown.store(value > 0 ? value : 0);
             return COSMOS_OK;
-        case COSMOS_TEST_TC_SKIP_MMA: {
+        case COSMOS_TEST_TC_SKIP_MMA:
+        case COSMOS_TEST_COPY_WAIT: {
             if (!h) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
-            if (!is_tc(h->cfg.force_mode)) return finish(h, cpm::fail(COSMOS_ERR_STATE, "not a tensor-core force mode"));
+            if (hook == COSMOS_TEST_TC_SKIP_MMA && !is_tc(h->cfg.force_mode))
+                return finish(h, cpm::fail(COSMOS_ERR_STATE, "not a tensor-core force mode"));
             DeviceGuard g(h->device);
             cudaStreamSynchronize(h->stream);
-            h->tc.skip_mma = value != 0;
+            if (hook == COSMOS_TEST_TC_SKIP_MMA)
+                h->tc.skip_mma = value != 0;
+            else
+                h->copy_tx_extra = value != 0 ? 16u : 0u;
             for (auto* set : {&h->graph, &h->graph_multi, &h->graph_prof})  // captured steps hold the old argument
                 for (auto& row : *set)
                     for (auto& gr : row)

@@ -1,14 +1,20 @@
-// Autotuner of the particle sort (cosmos_pm_autotune, include/cosmos_pm.h).
+// Autotuner of the step's launch shapes (cosmos_pm_autotune, include/cosmos_pm.h).
 //
 // The fused step kernel stages a tile's force window and deposit window in
 // shared memory, so its speed depends on the tile edge (the sort key
-// granularity) and on how far particles drift from their tile between
-// re-sorts (the sort cadence); the sort itself costs about three fused steps.
-// The best pair depends on the lattice, the particle count and how clustered
-// the state is, so it is measured on the caller's own state: every candidate
-// runs on a temporary handle, graph-launched, timed with CUDA events on the
-// handle's stream.  Results are cached in a plain text file, one line per key:
-//     N=<n> logP2=<2*log2(P) rounded> deposit=<0|1> force=<0|1> gpu=<name>|<gran> <interval> <ms>
+// granularity), on how far particles drift from their tile between re-sorts
+// (the sort cadence; the sort itself costs about three fused steps), on the
+// size of its work items and on how many CTAs share an SM; the spectral
+// column pass has two launch shapes (one or two radix-16 butterflies per
+// thread).  The best choice depends on the lattice, the particle count and
+// how clustered the state is, so it is measured on the caller's own state:
+// every candidate runs on a temporary handle, graph-launched, timed with CUDA
+// events on the handle's stream.  The search is coordinate-wise: tile edge x
+// cadence first, then the work-item size, the fused kernel's CTAs per SM and
+// the column-pass shape, each with the best of the ones before.  Results are
+// cached in a plain text file, one line per key:
+//     v2 N=<n> logP2=<2*log2(P) rounded> deposit=<0|1> force=<mode> gpu=<name>|
+//         <gran> <interval> <item_size> <ctas_per_sm> <fft_shape> <ms>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -28,12 +34,26 @@ std::mutex g_cache_mu;
 std::string cache_key(const cosmos_pm_config& c, const char* gpu) {
     const int logp2 = c.num_particles > 0 ? int(std::lround(2.0 * std::log2(double(c.num_particles)))) : 0;
     std::ostringstream k;
-    k << "N=" << c.lattice_n << " logP2=" << logp2 << " deposit=" << c.deposit << " force=" << c.force_mode
+    k << "v2 N=" << c.lattice_n << " logP2=" << logp2 << " deposit=" << c.deposit << " force=" << c.force_mode
       << " gpu=" << gpu;
     return k.str();
 }
 
-bool cache_lookup(const char* path, const std::string& key, int* gran, int* interval, float* ms) {
+// The tuned fields of a configuration, as one cache record.
+struct Choice {
+    int gran = 5, interval = 32, item = 0, ctas = 0, fft = 0;
+    float ms = 0.0f;
+};
+
+void apply(const Choice& ch, cosmos_pm_config* c) {
+    c->sort_granularity = ch.gran;
+    c->sort_interval = ch.interval;
+    c->item_size = ch.item;
+    c->fused_ctas_per_sm = ch.ctas;
+    c->fft_shape = ch.fft;
+}
+
+bool cache_lookup(const char* path, const std::string& key, Choice* out) {
     if (!path) return false;
     std::lock_guard<std::mutex> lk(g_cache_mu);
     std::ifstream f(path);
@@ -43,23 +63,21 @@ bool cache_lookup(const char* path, const std::string& key, int* gran, int* inte
         const size_t bar = line.rfind('|');
         if (bar == std::string::npos || line.compare(0, bar, key) != 0 || bar != key.size()) continue;
         std::istringstream v(line.substr(bar + 1));
-        int g = 0, i = 0;
-        float t = 0.0f;
-        if (v >> g >> i >> t) {
-            *gran = g;
-            *interval = i;
-            *ms = t;
+        Choice c;
+        if (v >> c.gran >> c.interval >> c.item >> c.ctas >> c.fft >> c.ms) {
+            *out = c;
             hit = true;
         }
     }
     return hit;
 }
 
-void cache_store(const char* path, const std::string& key, int gran, int interval, float ms) {
+void cache_store(const char* path, const std::string& key, const Choice& c) {
     if (!path) return;
     std::lock_guard<std::mutex> lk(g_cache_mu);
     std::ofstream f(path, std::ios::app);
-    f << key << '|' << gran << ' ' << interval << ' ' << ms << '\n';
+    f << key << '|' << c.gran << ' ' << c.interval << ' ' << c.item << ' ' << c.ctas << ' ' << c.fft << ' ' << c.ms
+      << '\n';
 }
 
 // Steps per second of one candidate: warm-up (prologue + first sort + graph
@@ -108,38 +126,66 @@ extern "C" int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, 
         if (ch == '|' || ch == '\n') ch = '_';
     const std::string key = cache_key(*base, gpu.c_str());
     *best = *base;
-    int g = 0, iv = 0;
-    float t = 0.0f;
-    if (cache_lookup(cache_path, key, &g, &iv, &t)) {
-        best->sort_granularity = g;
-        best->sort_interval = iv;
-        *best_ms = t;
+    Choice cur;
+    if (cache_lookup(cache_path, key, &cur)) {
+        apply(cur, best);
+        *best_ms = cur.ms;
         return COSMOS_OK;
     }
+    bool any = false;
+    // times `ch` (from the current best); keeps it when faster; false on a hard error in *rc
+    auto trial = [&](const Choice& ch, int* rc) -> bool {
+        cosmos_pm_config c = *base;
+        apply(ch, &c);
+        float ms = 0.0f;
+        *rc = time_candidate(c, x, y, xo, yo, m, steps, &ms);
+        if (*rc == COSMOS_ERR_NOMEM || *rc == COSMOS_ERR_INVALID) {  // a candidate that does not fit or apply
+            *rc = COSMOS_OK;
+            return true;
+        }
+        if (*rc != COSMOS_OK) return false;
+        if (!any || ms < cur.ms) {
+            cur = ch;
+            cur.ms = ms;
+            any = true;
+        }
+        return true;
+    };
+    int rc = COSMOS_OK;
+    // 1. tile edge x sort cadence (the other fields at their defaults)
     const int grans[] = {4, 5, 6};
     const int intervals[] = {8, 16, 24, 32, 48, 64, 0};
-    float best_t = 0.0f;
-    bool any = false;
     for (int gr : grans) {
         if ((base->lattice_n >> gr) < 1) continue;
         for (int itv : intervals) {
-            cosmos_pm_config c = *base;
-            c.sort_granularity = gr;
-            c.sort_interval = itv;
             if (itv == 0 && gr != grans[0]) continue;  // "never sort" ignores the tile edge
-            float ms = 0.0f;
-            const int rc = time_candidate(c, x, y, xo, yo, m, steps, &ms);
-            if (rc == COSMOS_ERR_NOMEM) continue;  // a candidate that does not fit is skipped
-            if (rc != COSMOS_OK) return rc;
-            if (!any || ms < best_t) {
-                best_t = ms;
-                *best = c;
-                any = true;
-            }
+            Choice ch;
+            ch.gran = gr;
+            ch.interval = itv;
+            if (!trial(ch, &rc)) return rc;
         }
     }
     if (!any) return cpm::fail(COSMOS_ERR_NOMEM, "autotune: no candidate fits on the device");
-    *best_ms = best_t;
-    cache_store(cache_path, key, best->sort_granularity, best->sort_interval, best_t);
+    // 2-4. work-item size, fused-kernel CTAs per SM, column-pass shape (tile order only)
+    if (cur.interval != 0) {
+        for (int item : {2048, 4096, 8192}) {
+            Choice ch = cur;
+            ch.item = item;
+            if (!trial(ch, &rc)) return rc;
+        }
+        for (int ctas : {2, 3}) {
+            Choice ch = cur;
+            ch.ctas = ctas;
+            if (!trial(ch, &rc)) return rc;
+        }
+    }
+    if (base->force_mode != COSMOS_FORCE_GRADIENT) {
+        Choice ch = cur;
+        ch.fft = 1;
+        if (!trial(ch, &rc)) return rc;
+    }
+    apply(cur, best);
+    *best_ms = cur.ms;
+    cache_store(cache_path, key, cur);
     return COSMOS_OK;
 }

@@ -76,6 +76,12 @@ struct cosmos_ensemble {
     bool density_valid = false, sort_due = true;
     int64_t steps_since_sort = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by buffer parity (all classes flip together)
+    // persistent step: grid size, barrier counter and status word, test hook
+    int persistent_grid = 0;
+    unsigned* barrier = nullptr;
+    int* pstatus = nullptr;
+    int skip_arrive = 0;
+    cpm::EnsStepArgs* pargs = nullptr;  // device: the step's arguments for buffer parity 0 and 1
     std::string err;
 };
 
@@ -147,6 +153,9 @@ void destroy_all(cosmos_ensemble* e) {
     for (auto& gr : e->graph)
         if (gr) cudaGraphExecDestroy(gr);
     for (auto& c : e->classes) destroy_class(c);
+    cudaFree(e->barrier);
+    cudaFree(e->pstatus);
+    cudaFree(e->pargs);
     if (e->start) cudaEventDestroy(e->start);
     if (e->stream) cudaStreamDestroy(e->stream);
 }
@@ -206,6 +215,29 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
     CPM_TRY(cpm::build_filter(c.N, e->cic, c.kq, c.tw, st));
     const uint64_t T = uint64_t(c.N >> c.gran);
     c.sort_bits = bits_for(uint64_t(c.nsims) * (T * T + 1) - 1);
+    return COSMOS_OK;
+}
+
+// The persistent step's arguments for both buffer parities (every class
+// flips its particle buffers together at a sort), in device memory.
+int upload_step_args(cosmos_ensemble* e) {
+    cpm::EnsStepArgs a[2] = {};
+    for (int parity = 0; parity < 2; ++parity) {
+        cpm::EnsStepArgs& x = a[parity];
+        x.nclasses = int(e->classes.size());
+        x.cic = e->cic;
+        x.g = e->cfg.gravity_multiplier;
+        x.dt = e->cfg.dt;
+        x.barrier = e->barrier;
+        x.status = e->pstatus;
+        x.skip_arrive = e->skip_arrive;
+        for (int i = 0; i < x.nclasses; ++i) {
+            EnsClass& c = e->classes[i];
+            x.cls[i] = cpm::EnsStepClass{c.N,  c.nsims, c.rho,   c.spec, c.spec2, c.edge,
+                                         c.dy, c.kq,    c.force, c.tw,   c.items, c.n_items, c.buf[parity]};
+        }
+    }
+    CPM_CUDA(cudaMemcpy(e->pargs, a, sizeof(a), cudaMemcpyHostToDevice));
     return COSMOS_OK;
 }
 
@@ -275,6 +307,20 @@ int create_impl(const cosmos_ensemble_config* cfg, const int32_t* ns, const int6
         if (rc != COSMOS_OK) return bail(rc);
         ++ci;
     }
+    if (cfg->persistent_step) {
+        if (cfg->force_mode != COSMOS_FORCE_SPECTRAL || e->classes.size() > size_t(cpm::kEnsMaxClasses))
+            return bail(cpm::fail(COSMOS_ERR_INVALID, "persistent_step needs the spectral force and at most 8 lattice sizes"));
+        for (auto& c : e->classes)
+            if (!cpm::ensemble_step_supported(c.N))
+                return bail(cpm::fail(COSMOS_ERR_INVALID, "persistent_step supports lattices of 128 to 1024"));
+        int rc = COSMOS_OK;
+        if ((rc = dalloc(&e->barrier, 1)) || (rc = dalloc(&e->pstatus, 1)) || (rc = dalloc(&e->pargs, 2)))
+            return bail(rc);
+        if (cudaMemsetAsync(e->pstatus, 0, sizeof(int), e->stream) != cudaSuccess ||
+            cpm::prepare_ensemble_step(e->nsm, &e->persistent_grid) != cudaSuccess)
+            return bail(cpm::fail(COSMOS_ERR_CUDA, "persistent step setup"));
+        if ((rc = upload_step_args(e)) != COSMOS_OK) return bail(rc);
+    }
     if (cudaStreamSynchronize(e->stream) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "create sync"));
     *out = e;
     return COSMOS_OK;
@@ -327,8 +373,17 @@ int class_body(cosmos_ensemble* e, EnsClass& c) {
     return COSMOS_OK;
 }
 
+// The step of every class as one persistent launch (pm_ensemble_step.cu),
+// with the arguments of the current buffer parity (upload_step_args).
+int step_body_persistent(cosmos_ensemble* e) {
+    const int parity = e->classes.empty() ? 0 : e->classes[0].cur;
+    CPM_CUDA(cpm::launch_ensemble_step(e->pargs + parity, e->barrier, e->persistent_grid, e->stream));
+    return COSMOS_OK;
+}
+
 // All classes: fork from the ensemble stream, run concurrently, join back.
 int step_body(cosmos_ensemble* e) {
+    if (e->cfg.persistent_step) return step_body_persistent(e);
     CPM_CUDA(cudaEventRecord(e->start, e->stream));
     for (auto& c : e->classes) {
         CPM_CUDA(cudaStreamWaitEvent(c.stream, e->start, 0));
@@ -530,6 +585,14 @@ int cosmos_ensemble_synchronize(cosmos_ensemble* e) {
     DeviceGuard g(e->device);
     auto impl = [&]() -> int {
         CPM_CUDA(cudaStreamSynchronize(e->stream));
+        if (e->pstatus) {  // a grid barrier of the persistent step that ran out
+            int st = 0;
+            CPM_CUDA(cudaMemcpy(&st, e->pstatus, sizeof(int), cudaMemcpyDeviceToHost));
+            if (st) {
+                CPM_CUDA(cudaMemset(e->pstatus, 0, sizeof(int)));
+                return cpm::fail(COSMOS_ERR_TIMEOUT, "persistent ensemble step: a grid barrier wait timed out");
+            }
+        }
         for (auto& c : e->classes) {  // a copy wait of a step kernel that gave up
             int st = 0;
             CPM_CUDA(cudaMemcpy(&st, c.status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -578,8 +641,17 @@ int cosmos_ensemble_launches_per_step(cosmos_ensemble* e, int32_t* launches) {
     if (!e || !launches) return cpm::fail(COSMOS_ERR_INVALID, "null argument");
     const int force = e->cfg.force_mode == COSMOS_FORCE_SPECTRAL ? cpm::spectral_launches_per_step()
                                                                  : cpm::conv_launches_per_step() + 1;
-    *launches = int32_t(e->classes.size()) * (force + 1);
+    *launches = e->cfg.persistent_step ? 1 : int32_t(e->classes.size()) * (force + 1);
     return COSMOS_OK;
+}
+
+int cosmos_ensemble_test_barrier(cosmos_ensemble* e, int32_t value) {
+    if (!e) return cpm::fail(COSMOS_ERR_INVALID, "null handle");
+    if (!e->cfg.persistent_step) return finish(e, cpm::fail(COSMOS_ERR_STATE, "not a persistent-step ensemble"));
+    DeviceGuard g(e->device);
+    cudaStreamSynchronize(e->stream);
+    e->skip_arrive = value != 0;
+    return finish(e, upload_step_args(e));
 }
 
 int cosmos_ensemble_stream(cosmos_ensemble* e, uint64_t* stream) {

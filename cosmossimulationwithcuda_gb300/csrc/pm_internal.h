@@ -55,7 +55,7 @@ cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2*
                                   const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
                                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1,
                                   const SpectralTc* tc = nullptr, float* clear = nullptr,
-                                  const SpectralMaps* maps = nullptr, int* status = nullptr);
+                                  const SpectralMaps* maps = nullptr, int* status = nullptr, int col_shape = 0);
 int spectral_launches_per_step();
 
 // pm_particles.cu
@@ -146,11 +146,41 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
                                int item_size, cudaStream_t st, int nsims = 1);
 // status: a bounded wait of the kernel that ran out sets *status (1: a wait
 // timed out; 2: copies were still in flight when the CTA gave up).
+// tx_extra: test hook (0 in normal use): bytes announced per copy stage that
+// never arrive, so the copy waits run out.
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
-                               int* status, cudaStream_t st);
+                               int* status, cudaStream_t st, uint32_t tx_extra = 0);
 cudaError_t launch_fused_global(const ParticleArrays& p, int64_t P, const float2* force, float* rho, int N, int cic,
                                 float dt, int nsm, cudaStream_t st);
+
+// pm_ensemble_step.cu -- the ensemble step as one persistent cooperative launch
+constexpr int kEnsMaxClasses = 8;
+struct EnsStepClass {  // one lattice class: nsims lattices of size N stored back to back
+    int N, nsims;
+    float* rho;
+    float2 *spec, *spec2, *edge;
+    float* dy;
+    const float* kq;
+    float2* force;
+    const float2* tw;
+    const WorkItem* items;
+    const uint32_t* n_items;
+    ParticleArrays p;  // the class's current particle buffer
+};
+struct EnsStepArgs {
+    int nclasses, cic;
+    float g, dt;
+    unsigned* barrier;  // grid-barrier arrival counter (zeroed by the launcher)
+    int* status;        // 4: a grid barrier ran out of time
+    int skip_arrive;    // test hook: CTA 0 does not arrive at the first barrier
+    EnsStepClass cls[kEnsMaxClasses];
+};
+bool ensemble_step_supported(int N);
+cudaError_t prepare_ensemble_step(int nsm, int* grid);
+// args_dev: the step's arguments in device memory (read by every CTA);
+// barrier: args_dev->barrier, zeroed on the stream before the launch.
+cudaError_t launch_ensemble_step(const EnsStepArgs* args_dev, unsigned* barrier, int grid, cudaStream_t st);
 
 // pm_ics.cu -- seeded initial conditions; particle i draws from (seed, first + i)
 cudaError_t launch_generate(const cosmos_ic_params& p, int64_t count, int64_t first, int N, float dt, float* x,

@@ -9,6 +9,8 @@
  * to back and every pass of the step (the FFT passes, the force, the fused
  * gather + update + deposit) covers all of them in one kernel launch; the
  * lattice sizes run concurrently on their own streams inside the graph.
+ * With persistent_step = 1 the step of all simulations is instead one
+ * persistent kernel launch (its phases separated by grid barriers).
  * Each simulation follows exactly the step of a cosmos_pm handle with the
  * same configuration (the same kernels, tile-sorted).
  *
@@ -37,7 +39,12 @@ typedef struct cosmos_ensemble_config {
     int32_t force_mode;        /* COSMOS_FORCE_GRADIENT / _SPECTRAL */
     int32_t sort_interval;     /* steps between tile re-sorts; <= 0: 32 */
     int32_t use_graph;         /* 1 = one captured CUDA graph per step */
-    int32_t reserved[8];
+    int32_t persistent_step;   /* 1 = the whole step of all simulations as ONE persistent
+                                  cooperative kernel launch (phases separated by bounded
+                                  grid barriers; spectral force, lattices 128..1024 and at
+                                  most 8 lattice sizes; create fails otherwise); 0 = one
+                                  kernel launch per pass and lattice size */
+    int32_t reserved[7];
 } cosmos_ensemble_config;
 
 typedef struct cosmos_ensemble cosmos_ensemble;
@@ -73,6 +80,12 @@ int cosmos_ensemble_get_field(cosmos_ensemble* e, int32_t sim, int32_t field, fl
  * on (a cudaStream_t as an integer). */
 int cosmos_ensemble_launches_per_step(cosmos_ensemble* e, int32_t* launches);
 int cosmos_ensemble_stream(cosmos_ensemble* e, uint64_t* stream);
+
+/* Test hook (persistent step): while value != 0 one CTA skips its arrival at
+ * the first grid barrier, so every barrier wait runs out; the next
+ * cosmos_ensemble_synchronize returns COSMOS_ERR_TIMEOUT and the handle stays
+ * usable (the step that gave up is incomplete). */
+int cosmos_ensemble_test_barrier(cosmos_ensemble* e, int32_t value);
 
 /* Message of the last error on this handle (or the last create failure when
  * e is NULL). */

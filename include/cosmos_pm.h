@@ -80,7 +80,17 @@ typedef struct cosmos_pm_config {
     int32_t sort_granularity;   /* log2 of the tile edge (cells) used as sort key; -1 = default */
     int32_t use_graph;          /* 1 = replay each step from a captured CUDA graph */
     int32_t blur_r;             /* render blur width, odd, 1..15 (Constants::BLUR_R, :49); 0 = 3 */
-    int32_t reserved[6];
+    /* Launch shapes (no counterpart in the reference, whose shapes are
+     * compile-time constants, CosmosCuda.cuh:29-74); 0 = library default.
+     * cosmos_pm_autotune picks them. */
+    int32_t item_size;          /* particles per work item of the fused step kernel: 2048, 4096 or
+                                   8192; 0 = chosen from the particle count */
+    int32_t fused_ctas_per_sm;  /* resident CTAs per SM of the fused step kernel's grid; 0 = as many
+                                   as fit */
+    int32_t fft_shape;          /* spectral modes: 0 = default column-pass shape, 1 = the other
+                                   shape (one radix-16 butterfly per thread per stage instead of two
+                                   from 1024^2 up, two instead of one below) */
+    int32_t reserved[3];
 } cosmos_pm_config;
 
 typedef struct cosmos_pm cosmos_pm; /* opaque handle (one Universe) */
@@ -258,13 +268,16 @@ int cosmos_pm_kernels_launched(cosmos_pm* h, int64_t* launches);
 
 /* ---- autotuning -----------------------------------------------------------
  * No counterpart in the reference (its launch shapes are compile-time
- * constants, CosmosCuda.cuh:29-74).  Searches the tile edge of the particle
- * sort (sort_granularity 4, 5, 6: 16, 32, 64 cells) and the re-sort cadence
- * (sort_interval 8, 16, 24, 32, 48, 64, or never) on the caller's own particle state:
- * each candidate runs on a temporary handle from the same host state, `steps`
- * graph-launched steps timed with CUDA events after a warm-up that includes
- * its first sort.  *best = *base with the fastest sort_granularity and
- * sort_interval; *best_ms = its time per step (amortising the sorts).
+ * constants, CosmosCuda.cuh:29-74).  Measures, on the caller's own particle
+ * state, the tile edge of the particle sort (sort_granularity 4, 5, 6: 16, 32,
+ * 64 cells) x the re-sort cadence (sort_interval 8, 16, 24, 32, 48, 64, or
+ * never), then with the best of those the work-item size of the fused step
+ * kernel (item_size 2048, 4096, 8192), its CTAs per SM (fused_ctas_per_sm 2,
+ * 3 or as many as fit) and, in the spectral modes, the column-pass shape
+ * (fft_shape 0, 1): each candidate runs on a temporary handle from the same
+ * host state, `steps` graph-launched steps timed with CUDA events after a
+ * warm-up that includes its first sort.  *best = *base with the fastest of
+ * these fields; *best_ms = its time per step (amortising the sorts).
  * cache_path (may be NULL): a text file of earlier results keyed by lattice
  * size, particle count (half-octave bucket), deposit, force mode and GPU
  * name; a hit returns the cached choice without running, a miss appends the
@@ -317,9 +330,16 @@ int cosmos_pm_steps_taken(cosmos_pm* h, int64_t* steps);
  *                          MMA and no completion signal while value != 0, so
  *                          its bounded waits run out: the next
  *                          cosmos_pm_synchronize returns COSMOS_ERR_TIMEOUT and
- *                          the handle stays usable. */
+ *                          the handle stays usable.
+ * COSMOS_TEST_COPY_WAIT:   while value != 0, the fused step kernel announces
+ *                          16 bytes more per particle-copy stage than it
+ *                          copies, so its bounded copy waits run out (no copy
+ *                          is left in flight): the next cosmos_pm_synchronize
+ *                          returns COSMOS_ERR_TIMEOUT and the handle stays
+ *                          usable (the step that gave up is incomplete). */
 #define COSMOS_TEST_FAIL_ALLOC 1
 #define COSMOS_TEST_TC_SKIP_MMA 2
+#define COSMOS_TEST_COPY_WAIT 3
 int cosmos_pm_test_hook(cosmos_pm* h, int32_t hook, int64_t value);
 
 /* Page-locked host memory for the asynchronous readbacks (the reference's

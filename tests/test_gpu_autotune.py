@@ -1,4 +1,5 @@
-"""cosmos_pm_autotune: the sort granularity / cadence search and its cache."""
+"""cosmos_pm_autotune: the launch-shape search (sort tile edge and cadence,
+work-item size, fused-kernel CTAs per SM, column-pass shape) and its cache."""
 import os
 
 import numpy as np
@@ -12,17 +13,21 @@ def test_autotune_picks_a_candidate_and_caches(tmp_path):
     N, P = 256, 200_000
     st = ics.exponential_disk(P, N, 0.002, seed=9, scale=N / 10)
     cache = str(tmp_path / "tune.txt")
-    g, itv, ms = _lib.autotune(st, N, dt=0.002, steps=16, cache_path=cache)
-    assert g in (4, 5, 6) and itv in (8, 16, 24, 32, 48, 64, 0) and ms > 0
+    best, ms = _lib.autotune(st, N, dt=0.002, steps=16, cache_path=cache)
+    assert best["sort_granularity"] in (4, 5, 6) and best["sort_interval"] in (8, 16, 24, 32, 48, 64, 0) and ms > 0
+    assert best["item_size"] in (0, 2048, 4096, 8192) and best["fused_ctas_per_sm"] in (0, 2, 3)
+    assert best["fft_shape"] in (0, 1)
     lines = open(cache).read().splitlines()
-    assert len(lines) == 1 and lines[0].startswith(f"N={N} ")
+    assert len(lines) == 1 and lines[0].startswith(f"v2 N={N} ")
     # a hit returns the stored choice and leaves the file alone
-    g2, itv2, ms2 = _lib.autotune(st, N, dt=0.002, steps=16, cache_path=cache)
-    assert (g2, itv2) == (g, itv) and abs(ms2 - ms) <= 1e-3 * ms + 1e-6
+    best2, ms2 = _lib.autotune(st, N, dt=0.002, steps=16, cache_path=cache)
+    assert best2 == best and abs(ms2 - ms) <= 1e-3 * ms + 1e-6
     assert open(cache).read().splitlines() == lines
     # the chosen configuration runs the same step
-    with _lib.Simulation(N, P, dt=0.002, force_mode=_lib.FORCE_SPECTRAL, sort_granularity=g if itv else -1,
-                         sort_interval=itv) as a, \
+    shape = dict(best)
+    if not shape["sort_interval"]:
+        shape["sort_granularity"] = -1
+    with _lib.Simulation(N, P, dt=0.002, force_mode=_lib.FORCE_SPECTRAL, **shape) as a, \
             _lib.Simulation(N, P, dt=0.002, force_mode=_lib.FORCE_SPECTRAL) as b:
         a.set_state(st)
         b.set_state(st)
@@ -32,6 +37,30 @@ def test_autotune_picks_a_candidate_and_caches(tmp_path):
     assert np.abs(xa - xb).max() <= 1e-4
 
 
+@pytest.mark.parametrize("shape", [dict(item_size=2048), dict(item_size=8192), dict(fused_ctas_per_sm=2),
+                                   dict(fft_shape=1)])
+def test_launch_shapes_run_the_same_step(shape):
+    """Every launch shape the tuner may pick runs the same step: NGP with
+    unit masses is bit-exact across the fused kernel's shapes (every density
+    sum is exact); the other column-pass shape sums the y-edge differences in
+    another order, so it agrees to 1e-5 cells."""
+    from cosmossimulationwithcuda_gb300 import _lib, ics
+    N, P, dt = 1024, 1 << 19, 0.002
+    st = ics.uniform(P, N, dt, seed=12)
+    out = []
+    for kw in (dict(), shape):
+        with _lib.Simulation(N, P, cic=False, dt=dt, force_mode=_lib.FORCE_SPECTRAL, sort_interval=4, **kw) as s:
+            s.set_state(st)
+            s.step(6)
+            s.synchronize()
+            out.append(s.get_particles())
+    for a, b in zip(*out):
+        if "fft_shape" in shape:
+            assert np.abs(a - b).max() <= 1e-5
+        else:
+            np.testing.assert_array_equal(a, b)
+
+
 def test_autotune_rejects_bad_arguments():
     from cosmossimulationwithcuda_gb300 import _lib, ics
     st = ics.uniform(1024, 64, 0.01, seed=1)
@@ -39,3 +68,7 @@ def test_autotune_rejects_bad_arguments():
         _lib.autotune(st, 64, dt=0.01, steps=0)
     with pytest.raises(_lib.CosmosError):
         _lib.autotune(st, 100, dt=0.01, steps=4)  # N not a power of two
+    with pytest.raises(_lib.CosmosError):
+        _lib.Simulation(64, 1024, item_size=1000)
+    with pytest.raises(_lib.CosmosError):
+        _lib.Simulation(64, 1024, fft_shape=2)

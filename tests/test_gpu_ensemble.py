@@ -135,7 +135,8 @@ def test_ensemble_rejects_bad_configs():
         assert ens.launches_per_step() == 2 * 6
 
 
-def test_ensemble_members_match_fp64_oracle():
+@pytest.mark.parametrize("persistent", [False, True])
+def test_ensemble_members_match_fp64_oracle(persistent):
     """Members of an ensemble at the batched form's lattice sizes (256^2,
     512^2, 1024^2) against the FP64 oracle on each member's own GPU
     positions: the fused kernel's deposit <= 1e-6, the force the next step
@@ -154,7 +155,8 @@ def test_ensemble_members_match_fp64_oracle():
             states.append(ics.exponential_disk(P, N, dt, seed=seed, scale=N / 10.0))
     Ns = [m[0] for m in members]
     Ps = [m[1] for m in members]
-    with _lib.Ensemble(Ns, Ps, cic=True, dt=dt, force_mode=_lib.FORCE_SPECTRAL, sort_interval=8) as ens:
+    with _lib.Ensemble(Ns, Ps, cic=True, dt=dt, force_mode=_lib.FORCE_SPECTRAL, sort_interval=8,
+                       persistent=persistent) as ens:
         for i, st in enumerate(states):
             ens.set_state(i, st)
         ens.step(5)
@@ -180,3 +182,90 @@ def test_ensemble_members_match_fp64_oracle():
         keep = (x > 3) & (x < N - 3) & (y > 3) & (y < N - 3)
         assert np.abs(after[i][0] - rx)[keep].max() <= 1e-3, i
         assert np.abs(after[i][1] - ry)[keep].max() <= 1e-3, i
+
+
+PERSISTENT_CASES = [(128, 20000, "uniform"), (256, 40000, "uniform"), (512, 100000, "uniform"), (1024, 200000, "uniform"),
+                    (256, 0, "uniform"), (512, 8000, "uniform")]
+
+
+def _unit_mass_states(dt):
+    from cosmossimulationwithcuda_gb300 import ics
+    return [ics.uniform(P, N, dt, seed=200 + i) if P else None for i, (N, P, _) in enumerate(PERSISTENT_CASES)]
+
+
+def _run_ensemble(persistent, steps, dt, cic=False, use_graph=True):
+    from cosmossimulationwithcuda_gb300 import _lib
+    states = _unit_mass_states(dt)
+    with _lib.Ensemble([c[0] for c in PERSISTENT_CASES], [c[1] for c in PERSISTENT_CASES], cic=cic, dt=dt,
+                       force_mode=_lib.FORCE_SPECTRAL, sort_interval=4, use_graph=use_graph,
+                       persistent=persistent) as ens:
+        if persistent:
+            assert ens.launches_per_step() == 1
+        for i, st in enumerate(states):
+            if st is not None:
+                ens.set_state(i, st)
+        ens.step(steps)
+        ens.synchronize()
+        return ([ens.get_particles(i) for i in range(len(PERSISTENT_CASES))],
+                [ens.get_field(i, _lib.FIELD_DENSITY) for i in range(len(PERSISTENT_CASES))])
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_persistent_step_equals_graph_step_ngp(use_graph):
+    """The one-launch persistent step runs the same bodies as the per-pass
+    kernels: NGP with unit masses (every density sum exact) gives the same
+    bits, including across re-sorts (sort every 4 steps, 9 steps)."""
+    a_p, a_d = _run_ensemble(False, 9, 0.002)
+    b_p, b_d = _run_ensemble(True, 9, 0.002, use_graph=use_graph)
+    for i in range(len(PERSISTENT_CASES)):
+        for x, y in zip(a_p[i], b_p[i]):
+            np.testing.assert_array_equal(x, y)
+        np.testing.assert_array_equal(a_d[i], b_d[i])
+
+
+def test_persistent_step_cic_close_to_graph_step():
+    a_p, a_d = _run_ensemble(False, 6, 0.002, cic=True)
+    b_p, b_d = _run_ensemble(True, 6, 0.002, cic=True)
+    for i, (N, P, _) in enumerate(PERSISTENT_CASES):
+        if P:
+            assert np.abs(a_p[i][0] - b_p[i][0]).max() <= 1e-4
+            assert rel_l2(b_d[i], a_d[i]) <= 1e-6
+
+
+def test_persistent_barrier_timeout_is_reported_and_recovers():
+    """A grid barrier of the persistent step that never completes (one CTA
+    skips its arrival) runs out after its bounded wait: every CTA returns, the
+    status reaches cosmos_ensemble_synchronize as COSMOS_ERR_TIMEOUT, and the
+    handle steps on normally once the hook is cleared."""
+    from cosmossimulationwithcuda_gb300 import _lib
+    dt = 0.002
+    states = _unit_mass_states(dt)
+    want = _run_ensemble(True, 2, dt)[0]
+    with _lib.Ensemble([c[0] for c in PERSISTENT_CASES], [c[1] for c in PERSISTENT_CASES], cic=False, dt=dt,
+                       force_mode=_lib.FORCE_SPECTRAL, sort_interval=4, persistent=True) as ens:
+        for i, st in enumerate(states):
+            if st is not None:
+                ens.set_state(i, st)
+        ens.test_barrier(1)
+        with pytest.raises(_lib.CosmosError) as err:
+            ens.step(1)
+            ens.synchronize()
+        assert err.value.code == -5  # COSMOS_ERR_TIMEOUT
+        ens.test_barrier(0)
+        for i, st in enumerate(states):  # the step that gave up is incomplete: start again
+            if st is not None:
+                ens.set_state(i, st)
+        ens.step(2)
+        ens.synchronize()
+        got = [ens.get_particles(i) for i in range(len(PERSISTENT_CASES))]
+    for i in range(len(PERSISTENT_CASES)):
+        for x, y in zip(got[i], want[i]):
+            np.testing.assert_array_equal(x, y)
+
+
+def test_persistent_step_rejects_unsupported_configs():
+    from cosmossimulationwithcuda_gb300 import _lib
+    with pytest.raises(_lib.CosmosError):
+        _lib.Ensemble([2048], [4096], persistent=True)  # lattice above 1024
+    with pytest.raises(_lib.CosmosError):
+        _lib.Ensemble([256], [4096], force_mode=_lib.FORCE_GRADIENT, persistent=True)

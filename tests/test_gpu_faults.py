@@ -133,3 +133,32 @@ def test_tc_wait_timeout_is_reported_and_recovers(cosmos_lib, rng):
         s.synchronize()  # the status was cleared and the context is usable
         got = s.get_field(cosmos_lib.FIELD_FORCE)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-5
+
+
+def test_copy_wait_timeout_is_reported_and_recovers(cosmos_lib):
+    """The fused step kernel's bounded copy waits: announced bytes that never
+    arrive make them run out; the status reaches cosmos_pm_synchronize as
+    COSMOS_ERR_TIMEOUT, and after the hook is cleared the handle steps on
+    exactly like a fresh one from the same state (NGP, unit masses)."""
+    from cosmossimulationwithcuda_gb300 import ics
+    N, P, dt = 256, 200_000, 0.002
+    st = ics.uniform(P, N, dt, seed=8)
+    with cosmos_lib.Simulation(N, P, cic=False, dt=dt, sort_interval=1) as ref:
+        ref.set_state(st)
+        ref.step(2)
+        ref.synchronize()
+        want = ref.get_particles()
+    with cosmos_lib.Simulation(N, P, cic=False, dt=dt, sort_interval=1) as s:
+        s.set_state(st)
+        s.test_hook(cosmos_lib.TEST_COPY_WAIT, 1)
+        with pytest.raises(cosmos_lib.CosmosError) as err:
+            s.step(1)
+            s.synchronize()
+        assert err.value.code == -5  # COSMOS_ERR_TIMEOUT
+        s.test_hook(cosmos_lib.TEST_COPY_WAIT, 0)
+        s.set_state(st)  # the step that gave up is incomplete: start again
+        s.step(2)
+        s.synchronize()  # the status was cleared and the context is usable
+        got = s.get_particles()
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
