@@ -529,7 +529,7 @@ def main():
                                                                      "autotune.txt"))
         os.makedirs(os.path.dirname(cache), exist_ok=True)
         t0 = time.perf_counter()
-        chosen, tms = _lib.autotune(state, N, cic=cic, dt=dt, device=local, force_mode=mode, steps=128,
+        chosen, tms = _lib.autotune(state, N, cic=cic, dt=dt, device=local, force_mode=mode, steps=256,
                                     cache_path=cache)
         shape = dict(chosen)
         if not shape["sort_interval"]:

@@ -284,26 +284,34 @@ __device__ __forceinline__ void cols_spectral_lines(const Src& src, float2* s, f
     fft_lines<N, 2 * B, NT, +1, C, kMaxRadix>(s, sload, gstore2, tw, 1);
 }
 
-// Body of the spectral C2R row pass: C2R of Fx = IFFT_x(i S(kx) g Phi) and
-// Fy = IFFT_x(Psi) for B rows (from y0), with the x-edge corrections from Phi,
-// written as interleaved (fx, fy).  spec / spec2 / force address one lattice;
-// s holds 2B padded lines followed by the block_sum scratch (NT/32 * 3B
-// floats); dx: 3B floats of shared scratch.  The y-edge corrections of rows
-// 0, 1, N-2, N-1 follow in apply_edge_rows.
+// Body of the spectral C2R row pass: Fx = IFFT_x(i S(kx) g Phi) and
+// Fy = IFFT_x(Psi) for B rows (from y0), with the x-edge corrections from
+// Phi, written as interleaved (fx, fy).  Both are real, so one N-point
+// complex inverse FFT of Z = X + i Y (X, Y the Hermitian spectra of Fx, Fy,
+// extended to k in [0, N) by X[N-k] = conj X[k]) gives z = fx + i fy directly,
+// the force's own (fx, fy) layout: no half-length pre-split and no
+// interleaving pass.  spec / spec2 / force address one lattice; s holds B
+// padded lines of N points (row b: Phi in [0, M), Psi in [M, N) until Z
+// replaces them) followed by the block_sum scratch (NT/32 * 3B floats);
+// dx: 3B floats of shared scratch.  The y-edge corrections of rows 0, 1,
+// N-2, N-1 follow in apply_edge_rows.
+template <int N>
+constexpr size_t c2r_spectral_line() { return size_t(LinePad<N>::value); }
+
 template <int N, int B, int NT>
 __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const float2* __restrict__ spec,
                                                   const float2* __restrict__ spec2, float4* __restrict__ force,
                                                   const float2* __restrict__ tw, float g, int y0) {
     using C = float2;
     constexpr int M = N / 2;
-    constexpr int LP = LinePad<M>::value;
-    float* red = reinterpret_cast<float*>(s + 2 * B * LP);
+    constexpr int LP = LinePad<N>::value;
+    float* red = reinterpret_cast<float*>(s + B * LP);
 #pragma unroll 4  // several transposed loads in flight per thread (measured: -2 us per step at 2048^2)
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
         const int b = idx - k * B;
         s[b * LP + pad16(k)] = spec[size_t(k) * N + y0 + b];
-        s[(B + b) * LP + pad16(k)] = spec2[size_t(k) * N + y0 + b];
+        s[b * LP + pad16(M + k)] = spec2[size_t(k) * N + y0 + b];
     }
     __syncthreads();
     // One pass over the potential half spectra Phi: the x-edge differences
@@ -332,34 +340,50 @@ __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const fl
             }
         }
     }
-    block_sum<NT, 3 * B>(acc, red);
+    block_sum<NT, 3 * B>(acc, red);  // ends with a barrier: the Fx spectra are complete
     if (threadIdx.x < B) {
         dx[3 * threadIdx.x + 0] = 2.0f * acc[3 * threadIdx.x + 0];
         dx[3 * threadIdx.x + 1] = 2.0f * acc[3 * threadIdx.x + 1];
         dx[3 * threadIdx.x + 2] = 2.0f * acc[3 * threadIdx.x + 2];
     }
-    c2r_presplit<M, NT>(s, 2 * B, tw);
-    __syncthreads();
-    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
-    auto sstore = [s](int line, int i, C v) { s[line * LP + pad16(i)] = v; };
-    fft_lines<M, 2 * B, NT, +1, C, kMaxRadix>(s, sload, sstore, tw, 2);
-    // interleave, with the x-edge corrections
-    const float c12 = g * (1.0f / 12.0f);
-    for (int idx = threadIdx.x; idx < M * B; idx += NT) {
-        const int b = idx / M;
-        const int i = idx - b * M;
-        const C fx = s[b * LP + pad16(i)];        // (Fx[2i], Fx[2i+1])
-        const C fy = s[(B + b) * LP + pad16(i)];  // (Fy[2i], Fy[2i+1])
-        float4 o = make_float4(fx.x, fy.x, fx.y, fy.y);
-        if (i == 0) {  // x = 0, 1
-            o.x += (-8.0f * dx[3 * b + 0] + dx[3 * b + 1]) * c12;
-            o.z += dx[3 * b + 2] * c12;
-        } else if (i == M - 1) {  // x = N-2, N-1
-            o.x += dx[3 * b + 1] * c12;
-            o.z += (dx[3 * b + 2] - 8.0f * dx[3 * b + 0]) * c12;
+    // Z of every row, in place: the pair (k, M - k) reads X, Y at k, M - k
+    // (elements k, M - k, M + k, N - k) and writes Z at k, N - k, M - k, M + k,
+    // the same four elements, so no other thread's input is overwritten.
+    // Element 0 of X and Y holds the packed real pair (X[0], X[M]).
+    constexpr int H = M / 2 + 1;
+    for (int idx = threadIdx.x; idx < H * B; idx += NT) {
+        const int b = idx / H;
+        const int k = idx - b * H;
+        C* row = s + b * LP;
+        if (k == 0) {
+            const C x = row[0], y = row[pad16(M)];
+            row[0] = cmake<C>(x.x, y.x);         // Z[0] = X[0] + i Y[0]
+            row[pad16(M)] = cmake<C>(x.y, y.y);  // Z[M] = X[M] + i Y[M]
+        } else {
+            const int k2 = M - k;
+            const C x1 = row[pad16(k)], y1 = row[pad16(M + k)];
+            const C x2 = row[pad16(k2)], y2 = row[pad16(M + k2)];
+            row[pad16(k)] = cmake<C>(x1.x - y1.y, x1.y + y1.x);          // Z[k] = X + iY
+            row[pad16(N - k)] = cmake<C>(x1.x + y1.y, y1.x - x1.y);      // Z[N-k] = conj X + i conj Y
+            if (k2 != k) {
+                row[pad16(k2)] = cmake<C>(x2.x - y2.y, x2.y + y2.x);
+                row[pad16(N - k2)] = cmake<C>(x2.x + y2.y, y2.x - x2.y);
+            }
         }
-        force[(size_t(y0 + b) * N) / 2 + i] = o;
     }
+    __syncthreads();
+    // z = fx + i fy, written straight from the last radix stage with the x-edge corrections
+    const float c12 = g * (1.0f / 12.0f);
+    float2* frow = reinterpret_cast<float2*>(force) + size_t(y0) * N;
+    auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
+    auto gstore = [frow, dx, c12](int line, int i, C v) {
+        if (i <= 1 || i >= N - 2) {
+            const float d01 = dx[3 * line + 0], d02 = dx[3 * line + 1], d13 = dx[3 * line + 2];
+            v.x += (i == 0 ? -8.0f * d01 + d02 : i == 1 ? d13 : i == N - 2 ? d02 : d13 - 8.0f * d01) * c12;
+        }
+        frow[size_t(line) * N + i] = v;
+    };
+    fft_lines<N, B, NT, +1, C, kMaxRadix>(s, sload, gstore, tw, 1);
 }
 
 // y-edge corrections of Fy on rows 0, 1, N-2, N-1 at column x from the three

@@ -109,6 +109,11 @@ struct cosmos_pm {
 
     bool profiling = false;
     cudaEvent_t ev[kNumEv] = {};
+    // profiled graph steps: the stage events sit on a side branch of the graph
+    cudaStream_t prof_stream = nullptr;
+    cudaEvent_t prof_fork[kNumEv] = {};
+    cudaEvent_t prof_join = nullptr;
+    bool prof_forked = false;
     bool have_times = false;
     bool prof_sorted = false, prof_prologue = false;
 
@@ -182,15 +187,29 @@ bool is_spectral(int mode) {
 }
 bool is_tc(int mode) { return mode == COSMOS_FORCE_SPECTRAL_TC_FP16 || mode == COSMOS_FORCE_SPECTRAL_TC_BF16; }
 
-// A profiling event: under stream capture an external event-record node of
-// the graph being captured (a plain record would only join streams inside
-// the capture), otherwise a plain record.
-cudaError_t record_profile_event(cudaEvent_t ev, cudaStream_t st) {
+// Profiling event i at the current point of stream st.  Direct launches: a
+// plain record.  Under stream capture (a profiled graph step): an external
+// event-record node on a side branch that depends on everything captured on
+// st so far, so that the kernels of the step keep their own edges (and their
+// programmatic, overlapping launches) and the event still marks the moment
+// the work before it completed.  The side branch rejoins st at the end of
+// the capture (join_profile_branch).
+cudaError_t record_profile_event(cosmos_pm* h, int i, cudaStream_t st) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    const cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
     if (e != cudaSuccess) return e;
-    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
-                                               : cudaEventRecord(ev, st);
+    if (cs != cudaStreamCaptureStatusActive) return cudaEventRecord(h->ev[i], st);
+    if ((e = cudaEventRecord(h->prof_fork[i], st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(h->prof_stream, h->prof_fork[i], 0)) != cudaSuccess) return e;
+    h->prof_forked = true;
+    return cudaEventRecordWithFlags(h->ev[i], h->prof_stream, cudaEventRecordExternal);
+}
+
+cudaError_t join_profile_branch(cosmos_pm* h, cudaStream_t st) {
+    if (!h->prof_forked) return cudaSuccess;
+    h->prof_forked = false;
+    const cudaError_t e = cudaEventRecord(h->prof_join, h->prof_stream);
+    return e != cudaSuccess ? e : cudaStreamWaitEvent(st, h->prof_join, 0);
 }
 
 // clear_rho: zero the density behind the row pass (the step clears it for the deposit that follows).
@@ -223,10 +242,10 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
     const float g = h->cfg.gravity_multiplier;
     if (is_spectral(h->cfg.force_mode)) {
         CPM_TRY(launch_spectral(h, st, true));
-        if (profile) CPM_CUDA(record_profile_event(h->ev[kEvForce], st));
+        if (profile) CPM_CUDA(record_profile_event(h, kEvForce, st));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(h->N, h->rho, h->spec, h->kq, h->phi, h->tw, st, 1, h->rho));
-        if (profile) CPM_CUDA(record_profile_event(h->ev[kEvForce], st));
+        if (profile) CPM_CUDA(record_profile_event(h, kEvForce, st));
         CPM_CUDA(cpm::launch_gradient(h->phi, h->force, h->N, g, st));
     }
     return COSMOS_OK;
@@ -239,7 +258,7 @@ int enqueue_force(cosmos_pm* h, cudaStream_t st, bool profile) {
 int enqueue_step_body(cosmos_pm* h, cudaStream_t st, bool profile) {
     ParticleArrays& p = state(h);
     auto rec = [&](int i) -> int {
-        if (profile) CPM_CUDA(record_profile_event(h->ev[i], st));
+        if (profile) CPM_CUDA(record_profile_event(h, i, st));
         return COSMOS_OK;
     };
     CPM_TRY(rec(kEvFft));
@@ -280,6 +299,8 @@ int get_graph(cosmos_pm* h, cudaGraphExec_t* out, int steps = 1, bool profile = 
         CPM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         int rc = COSMOS_OK;
         for (int i = 0; i < steps && rc == COSMOS_OK; ++i) rc = enqueue_step_body(h, h->stream, profile);
+        if (rc == COSMOS_OK && join_profile_branch(h, h->stream) != cudaSuccess)
+            rc = cpm::fail(COSMOS_ERR_CUDA, "profile branch join");
         const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
         if (rc != COSMOS_OK) {
             if (graph) cudaGraphDestroy(graph);
@@ -461,6 +482,10 @@ void destroy_all(cosmos_pm* h) {
     cudaFree(h->n_items);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : h->prof_fork)
+        if (e) cudaEventDestroy(e);
+    if (h->prof_join) cudaEventDestroy(h->prof_join);
+    if (h->prof_stream) cudaStreamDestroy(h->prof_stream);
     for (auto& t : h->tickets) cudaEventDestroy(t.second);
     for (auto e : h->event_pool) cudaEventDestroy(e);
     if (h->fork_ev) cudaEventDestroy(h->fork_ev);
@@ -532,6 +557,12 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return bail(cpm::fail(COSMOS_ERR_CUDA, "stream creation"));
     for (auto& e : h->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "event creation"));
+    for (auto& e : h->prof_fork)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(cpm::fail(COSMOS_ERR_CUDA, "event creation"));
+    if (cudaEventCreateWithFlags(&h->prof_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->prof_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(cpm::fail(COSMOS_ERR_CUDA, "profiling stream"));
     for (int i = 0; i < 2; ++i) {
         if (cudaEventCreateWithFlags(&h->stage_ready[i], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->stage_done[i], cudaEventDisableTiming) != cudaSuccess)

@@ -9,9 +9,11 @@
 // thread).  The best choice depends on the lattice, the particle count and
 // how clustered the state is, so it is measured on the caller's own state:
 // every candidate runs on a temporary handle, graph-launched, timed with CUDA
-// events on the handle's stream.  The search is coordinate-wise: tile edge x
-// cadence first, then the work-item size, the fused kernel's CTAs per SM and
-// the column-pass shape, each with the best of the ones before.  Results are
+// events on the handle's stream.  The library's defaults are timed first; the
+// search is coordinate-wise: tile edge x cadence, then the work-item size, the
+// fused kernel's CTAs per SM and the column-pass shape, each with the best of
+// the ones before, and a candidate is taken only when it is more than 1.5%
+// faster than the best so far.  Results are
 // cached in a plain text file, one line per key:
 //     v2 N=<n> logP2=<2*log2(P) rounded> deposit=<0|1> force=<mode> gpu=<name>|
 //         <gran> <interval> <item_size> <ctas_per_sm> <fft_shape> <ms>
@@ -133,7 +135,11 @@ extern "C" int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, 
         return COSMOS_OK;
     }
     bool any = false;
-    // times `ch` (from the current best); keeps it when faster; false on a hard error in *rc
+    // A candidate replaces the best so far only when it is faster by more than
+    // kMargin: differences below that are within the run-to-run spread of a
+    // timing window and would not hold on a longer run.
+    constexpr float kMargin = 0.015f;
+    // times `ch`; keeps it when faster; false on a hard error in *rc
     auto trial = [&](const Choice& ch, int* rc) -> bool {
         cosmos_pm_config c = *base;
         apply(ch, &c);
@@ -144,7 +150,7 @@ extern "C" int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, 
             return true;
         }
         if (*rc != COSMOS_OK) return false;
-        if (!any || ms < cur.ms) {
+        if (!any || ms < cur.ms * (1.0f - kMargin)) {
             cur = ch;
             cur.ms = ms;
             any = true;
@@ -152,6 +158,12 @@ extern "C" int cosmos_pm_autotune(const cosmos_pm_config* base, const float* x, 
         return true;
     };
     int rc = COSMOS_OK;
+    {  // the library's defaults first: the reference every candidate has to beat
+        Choice def;
+        def.gran = base->sort_granularity;
+        def.interval = base->sort_interval;
+        if (!trial(def, &rc)) return rc;
+    }
     // 1. tile edge x sort cadence (the other fields at their defaults)
     const int grans[] = {4, 5, 6};
     const int intervals[] = {8, 16, 24, 32, 48, 64, 0};

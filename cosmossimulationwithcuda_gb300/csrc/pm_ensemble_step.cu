@@ -48,7 +48,7 @@ struct EnsShape {
     static constexpr size_t r2c_smem = size_t(RB) * LinePad<M>::value * sizeof(float2);
     static constexpr size_t col_smem = 2 * size_t(CB) * LinePad<N>::value * sizeof(float2) + (kEnsThreads / 32) * 6 * 4;
     static constexpr size_t c2r_smem =
-        2 * size_t(QB) * LinePad<M>::value * sizeof(float2) + (kEnsThreads / 32) * 3 * QB * 4 + 3 * QB * 4;
+        size_t(QB) * LinePad<N>::value * sizeof(float2) + (kEnsThreads / 32) * 3 * QB * 4 + 3 * QB * 4;
     static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
     static constexpr size_t smem = r2c_smem > col_smem ? (r2c_smem > c2r_smem ? r2c_smem : c2r_smem)
                                                         : (col_smem > c2r_smem ? col_smem : c2r_smem);
@@ -131,7 +131,7 @@ __device__ __noinline__ void do_c2r(const EnsStepClass& c, float g, int u, float
     constexpr int per = N / S::QB + 3;
     const int lat = u / per, r = u - lat * per;
     if (r < N / S::QB) {  // force rows
-        float* dx = reinterpret_cast<float*>(s + 2 * S::QB * LinePad<S::M>::value) + (kEnsThreads / 32) * 3 * S::QB;
+        float* dx = reinterpret_cast<float*>(s + S::QB * LinePad<N>::value) + (kEnsThreads / 32) * 3 * S::QB;
         const size_t off = size_t(lat) * S::M * N;
         c2r_spectral_rows<N, S::QB, kEnsThreads>(s, dx, c.spec + off, c.spec2 + off,
                                                  reinterpret_cast<float4*>(c.force) + off, c.tw, g, r * S::QB);

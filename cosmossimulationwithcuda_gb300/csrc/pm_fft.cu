@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
 // Rows, spectral force: C2R of Fx and Fy with the x-edge corrections
 // (c2r_spectral_rows, fft_passes.cuh).
 template <int N, int B, int NT>
-__global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N / 2>::value * sizeof(float2),
+__global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N>::value * sizeof(float2),
                                                  CPM_C2R_SPECTRAL_MINB, (N <= 512 ? 64 : 128)>::value))
     k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
@@ -365,16 +365,17 @@ struct SpecShape {
     using CS = ColShape<float, N>;
     static constexpr int M = N / 2;
     static constexpr int RB0 = RS::B;
-    static constexpr size_t row_bytes0 = 2 * size_t(RB0) * LinePad<M>::value * sizeof(float2);
+    static constexpr size_t row_bytes0 = size_t(RB0) * LinePad<N>::value * sizeof(float2);
     static constexpr int RB = row_bytes0 > 200 * 1024 ? RB0 / 2 : RB0;  // rows per CTA
-    // Up to 512^2 one butterfly per thread per stage (2 RB lines; 64 registers
-    // a thread), above that two (128 registers): measured 43 -> 39 us for the
-    // 512^2 force passes, and 83 -> 86 us at 2048^2 the other way round.
+    // Up to 512^2 one butterfly per thread per stage (RB lines of N points; 64
+    // registers a thread), above that two (128 registers): measured 43 -> 39 us
+    // for the 512^2 force passes, and 83 -> 86 us at 2048^2 the other way round.
     static constexpr int RNT0 = (N <= 512 ? 2 : 1) * RB * M / kMaxRadix;
     static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
-    // two spectra per row, plus block_sum scratch: one slot per warp for each of the 3 * RB edge sums
+    // one N-point line per row (the two half spectra, then Z), plus block_sum
+    // scratch: one slot per warp for each of the 3 * RB edge sums
     static constexpr size_t row_smem =
-        2 * size_t(RB) * LinePad<M>::value * sizeof(float2) + size_t(RNT / 32) * 3 * RB * sizeof(float);
+        size_t(RB) * LinePad<N>::value * sizeof(float2) + size_t(RNT / 32) * 3 * RB * sizeof(float);
     // column pass threads of one lattice: one butterfly per thread in the
     // inverse transforms (2 B lines) up to CPM_COLS_FULL_MAX_N; batches of
     // lattices keep CS::NT (measured faster for the ensemble's 512^2 class)

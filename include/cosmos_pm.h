@@ -249,7 +249,10 @@ int cosmos_pm_diagnostics(cosmos_pm* h, double* kinetic, double* potential, doub
  * stencil (gradient mode), fused gather + update + deposit, tile sort (0 when
  * the step did not sort).  A profiled step runs as one step per graph launch
  * (direct launches when graphs are off) with events recorded between its
- * stages; the prologue and the sort run before it as direct launches.
+ * stages, on a side branch of the graph so that the step's kernels keep
+ * their overlapping (programmatic) launches: a stage time is the time from
+ * the completion of the stage before to the completion of this one.  The
+ * prologue and the sort run before the step as direct launches.
  * *n = capacity on entry, entries written on return. */
 int cosmos_pm_set_profiling(cosmos_pm* h, int32_t enabled);
 int cosmos_pm_stage_times(cosmos_pm* h, float* times, int32_t* n);
@@ -276,8 +279,10 @@ int cosmos_pm_kernels_launched(cosmos_pm* h, int64_t* launches);
  * 3 or as many as fit) and, in the spectral modes, the column-pass shape
  * (fft_shape 0, 1): each candidate runs on a temporary handle from the same
  * host state, `steps` graph-launched steps timed with CUDA events after a
- * warm-up that includes its first sort.  *best = *base with the fastest of
- * these fields; *best_ms = its time per step (amortising the sorts).
+ * warm-up that includes its first sort.  The library's defaults are timed
+ * first and a candidate is taken only when it is more than 1.5% faster than
+ * the best so far.  *best = *base with the chosen fields; *best_ms = its time
+ * per step (amortising the sorts).
  * cache_path (may be NULL): a text file of earlier results keyed by lattice
  * size, particle count (half-octave bucket), deposit, force mode and GPU
  * name; a hit returns the cached choice without running, a miss appends the
