@@ -49,6 +49,24 @@ __device__ __forceinline__ void copy_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// L2 policy for data read once per step (the particle state): evicted first,
+// so that it does not push the step's lattices out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// copy_g2s with an L2 cache-eviction policy for the source lines.
+__device__ __forceinline__ void copy_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
 __device__ __forceinline__ bool try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(

@@ -60,6 +60,11 @@ struct ColShape {
 #ifndef CPM_COLS_FULL_MAX_N
 #define CPM_COLS_FULL_MAX_N 512
 #endif
+// Up to this lattice size the spectral C2R row pass runs one butterfly per
+// thread per stage (twice the threads).
+#ifndef CPM_C2R_FULL_MAX_N
+#define CPM_C2R_FULL_MAX_N 512
+#endif
 
 
 // Minimum resident CTAs per SM for a block size (register limit of launch bounds).

@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
 // (c2r_spectral_rows, fft_passes.cuh).
 template <int N, int B, int NT>
 __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N>::value * sizeof(float2),
-                                                 CPM_C2R_SPECTRAL_MINB, (N <= 512 ? 64 : 128)>::value))
+                                                 CPM_C2R_SPECTRAL_MINB, (N <= CPM_C2R_FULL_MAX_N ? 64 : 128)>::value))
     k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
                                                              float4* __restrict__ force,
@@ -370,7 +370,7 @@ struct SpecShape {
     // Up to 512^2 one butterfly per thread per stage (RB lines of N points; 64
     // registers a thread), above that two (128 registers): measured 43 -> 39 us
     // for the 512^2 force passes, and 83 -> 86 us at 2048^2 the other way round.
-    static constexpr int RNT0 = (N <= 512 ? 2 : 1) * RB * M / kMaxRadix;
+    static constexpr int RNT0 = (N <= CPM_C2R_FULL_MAX_N ? 2 : 1) * RB * M / kMaxRadix;
     static constexpr int RNT = RNT0 < 64 ? 64 : (RNT0 > 1024 ? 1024 : RNT0);
     // one N-point line per row (the two half spectra, then Z), plus block_sum
     // scratch: one slot per warp for each of the 3 * RB edge sums

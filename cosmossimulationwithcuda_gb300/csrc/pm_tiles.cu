@@ -187,6 +187,11 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
 // Waits are bounded: a timeout sets *status, the CTA stops issuing work,
 // every warp keeps its barrier schedule with the work skipped, and the
 // producer waits (bounded) for its copies in flight before the CTA exits.
+// CPM_BULK_EVICT_FIRST=1 reads the particle chunks with an L2 evict-first
+// policy (measured: 0.2602 -> 0.2617 ms per step at 20M / 2048^2, so off).
+#ifndef CPM_BULK_EVICT_FIRST
+#define CPM_BULK_EVICT_FIRST 0
+#endif
 constexpr int kBulkConsumers = 256;                    // 8 compute warps
 constexpr int kBulkThreads = kBulkConsumers + 32;      // + 1 producer warp
 constexpr int kBulkChunk = 4 * kBulkConsumers;         // particles per stage: one float4 group per thread
@@ -224,6 +229,9 @@ __global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkIte
     if (warp == kBulkConsumers / 32) {  // ---- producer warp: one lane issues the copies ----
         if (lane != 0) return;
         float* const arr[kBulkArrays] = {p.x, p.y, p.xo, p.yo, p.m};
+#if CPM_BULK_EVICT_FIRST
+        const uint64_t policy = bulk::l2_evict_first_policy();
+#endif
         uint32_t fills[kBulkStages] = {};
         uint32_t fill = 0;
         for (uint32_t it = blockIdx.x; it < n_items && !abort_flag; it += gridDim.x) {
@@ -242,7 +250,12 @@ __global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkIte
                 bulk::arrive_expect_tx(&full[s], n * 4u * kBulkArrays + tx_extra);
                 float* st = stages + size_t(s) * kBulkStageFloats;
 #pragma unroll
-                for (int a = 0; a < kBulkArrays; ++a) bulk::copy_g2s(st + a * kBulkChunk, arr[a] + c, n * 4u, &full[s]);
+                for (int a = 0; a < kBulkArrays; ++a)
+#if CPM_BULK_EVICT_FIRST
+                    bulk::copy_g2s_hint(st + a * kBulkChunk, arr[a] + c, n * 4u, &full[s], policy);
+#else
+                    bulk::copy_g2s(st + a * kBulkChunk, arr[a] + c, n * 4u, &full[s]);
+#endif
                 ++fills[s];
             }
         }
