@@ -56,7 +56,7 @@ struct EnsShape {
 constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
 constexpr size_t kEnsSmem =
     cmax(cmax(cmax(EnsShape<128>::smem, EnsShape<256>::smem), cmax(EnsShape<512>::smem, EnsShape<1024>::smem)),
-         size_t(win_y(kEnsGran)) * win_x(kEnsGran) * (sizeof(float2) + sizeof(uint32_t)));
+         cmax(window_bytes(kEnsGran, 0), window_bytes(kEnsGran, 1)));
 
 __device__ __forceinline__ uint64_t gtimer_ns() {
     uint64_t t;
@@ -200,8 +200,6 @@ __device__ __noinline__ void fft_phase(const EnsStepArgs& a, int phase, float2* 
 }
 
 __device__ __noinline__ void fused_phase(const EnsStepArgs& a, float2* s) {
-    float2* fwin = s;
-    uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + win_y(kEnsGran) * win_x(kEnsGran));
     uint32_t base = 0;
     for (int ci = 0; ci < a.nclasses; ++ci) {
         const EnsStepClass& c = a.cls[ci];
@@ -214,9 +212,9 @@ __device__ __noinline__ void fused_phase(const EnsStepArgs& a, float2* s) {
             const float2* force = c.force + size_t(item.sim) * c.N * c.N;
             float* rho = c.rho + size_t(item.sim) * c.N * c.N;
             if (a.cic)
-                fused_item<1, kEnsGran>(item, c.p, force, rho, c.N, a.dt, fwin, dwin);
+                fused_item<1, kEnsGran>(item, c.p, force, rho, c.N, a.dt, WindowSmem<1, kEnsGran>(s));
             else
-                fused_item<0, kEnsGran>(item, c.p, force, rho, c.N, a.dt, fwin, dwin);
+                fused_item<0, kEnsGran>(item, c.p, force, rho, c.N, a.dt, WindowSmem<0, kEnsGran>(s));
         }
         base += n;
     }

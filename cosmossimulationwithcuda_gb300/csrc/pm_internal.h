@@ -132,7 +132,7 @@ struct WorkItem {
 };
 // Elements of the tile-range arrays (tstart / tend) for nsims simulations.
 size_t tile_range_elems(int N, int gran, int nsims);
-size_t tile_window_smem(int gran);
+size_t tile_window_smem(int gran, int cic);
 // Work-item size for Pq particles: the largest of kItemMax, kItemMax / 2, ...
 // that still gives about four items per resident CTA (16 per SM), so that the
 // items of a smaller state still spread over the GPU; kItemMin below that.

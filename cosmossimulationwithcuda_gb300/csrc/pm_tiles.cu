@@ -156,10 +156,8 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
                                                                const uint32_t* __restrict__ n_items_p,
                                                                ParticleArrays p, const float2* __restrict__ force,
                                                                float* __restrict__ rho, int N, float dt) {
-    constexpr int WY = win_y(GRAN), WX = win_x(GRAN);
     extern __shared__ float4 smem4[];
-    float2* fwin = reinterpret_cast<float2*>(smem4);
-    uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
+    const WindowSmem<CIC, GRAN> win(smem4);
     dependency_wait();
     allow_dependents();
     const uint32_t n_items = *n_items_p;
@@ -168,7 +166,7 @@ __global__ void CPM_FUSED_BOUNDS k_fused_tiles(const WorkItem* __restrict__ item
     for (uint32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
         const WorkItem item = items[it];
         fused_item<CIC, GRAN>(item, p, force0 + size_t(item.sim) * N * N, rho0 + size_t(item.sim) * N * N, N, dt,
-                              fwin, dwin);
+                              win);
     }
 }
 
@@ -208,8 +206,7 @@ __global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkIte
     constexpr int WY = win_y(GRAN), WX = win_x(GRAN);
     extern __shared__ float4 smem4[];
     float* stages = reinterpret_cast<float*>(smem4);  // [stage][array][kBulkChunk]
-    float2* fwin = reinterpret_cast<float2*>(stages + kBulkStages * kBulkStageFloats);
-    uint32_t* dwin = reinterpret_cast<uint32_t*>(fwin + WY * WX);
+    const WindowSmem<CIC, GRAN> win(stages + kBulkStages * kBulkStageFloats);
     __shared__ __align__(8) uint64_t full[kBulkStages], empty[kBulkStages];
     __shared__ volatile int abort_flag;
     const int tid = int(threadIdx.x), warp = tid >> 5, lane = tid & 31;
@@ -275,18 +272,11 @@ __global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkIte
         rho = rho0 + size_t(item.sim) * N * N;
         const bool dense = item.end - item.begin >= uint32_t(kItemDirect);
         if (dense) {
-            for (int i = tid; i < WY * WX; i += kBulkConsumers) {
-                const int r = i / WX, c = i - r * WX;
-                const int gx = item.x0 + c, gy = item.y0 + r;
-                float2 f = make_float2(0.0f, 0.0f);
-                if (gx >= 0 && gx < N && gy >= 0 && gy < N) f = __ldg(force + size_t(gy) * N + gx);
-                fwin[i] = f;
-                dwin[i] = 0u;
-            }
+            stage_windows<CIC, GRAN>(item, force, N, win, tid, kBulkConsumers);
             bulk::named_sync(kBulkConsumers);
         }
-        const Window w = dense ? Window{fwin, dwin, item.x0, item.y0, item.scale, item.heavy}
-                               : Window{nullptr, nullptr, item.x0, item.y0, 1.0f, 0.0f};
+        const Window<CIC> w = dense ? Window<CIC>{win.f, win.d, item.x0, item.y0, item.scale, item.heavy}
+                                    : Window<CIC>{nullptr, nullptr, item.x0, item.y0, 1.0f, 0.0f};
         const uint32_t b = item.begin, e = item.end;
         const uint32_t b4 = (b + 3u) & ~3u, e4 = e & ~3u;
         if (!abort_flag) {  // ragged head / tail (or the whole range when it spans no full group)
@@ -332,19 +322,7 @@ __global__ void __launch_bounds__(kBulkThreads) k_fused_tiles_bulk(const WorkIte
         }
         if (dense) {
             bulk::named_sync(kBulkConsumers);
-            constexpr int W4 = WX / 4;
-            const uint4* d4 = reinterpret_cast<const uint4*>(dwin);
-            const float inv = item.inv_scale;
-            for (int i = tid; i < WY * W4 && !abort_flag; i += kBulkConsumers) {
-                const int r = i / W4, c4 = i - r * W4;
-                const int gy = item.y0 + r, gx = item.x0 + 4 * c4;
-                if (gy < 0 || gy >= N || gx < 0 || gx >= N) continue;
-                const uint4 q = d4[i];
-                if ((q.x | q.y | q.z | q.w) != 0u)
-                    red_add_v4(rho + size_t(gy) * N + gx,
-                               make_float4(__uint2float_rn(q.x) * inv, __uint2float_rn(q.y) * inv,
-                                           __uint2float_rn(q.z) * inv, __uint2float_rn(q.w) * inv));
-            }
+            if (!abort_flag) flush_window<CIC, GRAN>(item, rho, N, win, tid, kBulkConsumers);
             bulk::named_sync(kBulkConsumers);
         }
     }
@@ -360,7 +338,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p
     float4* XO = reinterpret_cast<float4*>(p.xo);
     float4* YO = reinterpret_cast<float4*>(p.yo);
     const float4* Mm = reinterpret_cast<const float4*>(p.m);
-    const Window w{nullptr, nullptr, 0, 0, 1.0f, 0.0f};
+    const Window<CIC> w{nullptr, nullptr, 0, 0, 1.0f, 0.0f};
     dependency_wait();
     for (int64_t g = blockIdx.x * int64_t(kFusedThreads) + threadIdx.x; g < ngroups;
          g += int64_t(gridDim.x) * kFusedThreads) {
@@ -378,7 +356,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_global(ParticleArrays p
 }
 
 // ---- host side -------------------------------------------------------------------------------
-size_t tile_window_smem(int gran) { return size_t(win_y(gran)) * win_x(gran) * (sizeof(float2) + sizeof(uint32_t)); }
+size_t tile_window_smem(int gran, int cic) { return window_bytes(gran, cic); }
 
 int work_item_size(int64_t Pq, int nsm) {
     const int64_t want = 16 * int64_t(nsm > 0 ? nsm : 152);
@@ -394,8 +372,8 @@ size_t max_work_items(int64_t Pq, int ntiles, int item_size) { return size_t(Pq 
 #ifndef CPM_FUSED_BULK
 #define CPM_FUSED_BULK 1
 #endif
-size_t fused_tiles_smem(int gran) {
-    return (CPM_FUSED_BULK ? size_t(kBulkStages) * kBulkStageFloats * sizeof(float) : 0) + tile_window_smem(gran);
+size_t fused_tiles_smem(int gran, int cic) {
+    return (CPM_FUSED_BULK ? size_t(kBulkStages) * kBulkStageFloats * sizeof(float) : 0) + tile_window_smem(gran, cic);
 }
 constexpr int kFusedLaunchThreads = CPM_FUSED_BULK ? kBulkThreads : kFusedThreads;
 
@@ -411,7 +389,7 @@ static auto fused_kernel() {
 cudaError_t prepare_tile_kernels(int gran, int cic, int nsm, int* grid) {
     cudaError_t e = cudaErrorInvalidValue;
     int per_sm = 0;
-    const size_t smem = fused_tiles_smem(gran);
+    const size_t smem = fused_tiles_smem(gran, cic);
 #define CPM_TILES(C, G)                                                                                        \
     if (cic == C && gran == G) {                                                                               \
         e = cudaFuncSetAttribute(fused_kernel<C, G>(), cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); \
@@ -452,7 +430,7 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
 cudaError_t launch_fused_tiles(const WorkItem* items, const uint32_t* n_items, const ParticleArrays& p,
                                const float2* force, float* rho, int N, int cic, float dt, int gran, int grid,
                                int* status, cudaStream_t st, uint32_t tx_extra) {
-    const size_t smem = fused_tiles_smem(gran);
+    const size_t smem = fused_tiles_smem(gran, cic);
 #if CPM_FUSED_BULK
 #define CPM_TILES(C, G)                                                                                      \
     if (cic == C && gran == G) {                                                                             \
