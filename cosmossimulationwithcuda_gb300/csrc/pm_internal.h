@@ -112,7 +112,12 @@ cudaError_t launch_diagnostics(const ParticleArrays& p, int64_t P, const float* 
                                cudaStream_t st);
 
 // pm_tiles.cu -- tile-ordered fused gather + update + next-step deposit
-constexpr int kTileHalo = 4;    // cells of drift tolerated around a tile's window
+#ifndef CPM_TILE_HALO
+#define CPM_TILE_HALO 4
+#endif
+constexpr int kTileHalo = CPM_TILE_HALO;  // cells of drift tolerated around a tile's window
+// Window origins stay on 4-cell boundaries (16-byte vector flushes of the density).
+static_assert(kTileHalo % 4 == 0, "tile halo must be a multiple of 4 cells");
 #ifndef CPM_ITEM_MAX
 #define CPM_ITEM_MAX 8192
 #endif
