@@ -104,6 +104,9 @@ __device__ __forceinline__ void r2c_rows(const Src& src, cplx_t<T>* s, cplx_t<T>
         for (int i = threadIdx.x; i < B * M; i += NT) z[i] = cmake<C>(T(0), T(0));
     }
     // X[k] = (Z[k] + conj Z[M-k])/2 - i/2 W^k (Z[k] - conj Z[M-k]),  W = exp(-2 pi i/N)
+    // (unrolled: several twiddle loads and transposed stores in flight per
+    // thread, measured -1 us per step at 2048^2)
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
         const int k = idx / B;
         const int b = idx - k * B;
