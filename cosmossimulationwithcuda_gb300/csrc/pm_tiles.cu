@@ -50,13 +50,37 @@ __device__ __forceinline__ uint32_t compact_bits(uint32_t v) {
 }  // namespace
 
 // ---- work items from the sorted keys -------------------------------------------------------
+// Tile ranges of the sorted keys: a tile's range starts where its key differs
+// from the one before and ends where it differs from the one after.  One
+// thread takes four consecutive keys with one 16-byte load (the key buffers
+// are 16-byte aligned) plus the keys either side.
 __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, int64_t n, uint32_t ntiles,
                               uint32_t* __restrict__ tstart, uint32_t* __restrict__ tend) {
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-        const uint32_t k = keys[i];
-        if (k >= ntiles) continue;
-        if (i == 0 || keys[i - 1] != k) tstart[k] = uint32_t(i);
-        if (i == n - 1 || keys[i + 1] != k) tend[k] = uint32_t(i + 1);
+    constexpr uint32_t kNone = 0xFFFFFFFFu;  // no key: before the first one and after the last one
+    const int64_t nq = (n + 3) / 4;
+    for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < nq; q += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i0 = q * 4;
+        uint32_t k[6];
+        if (i0 + 4 <= n) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(keys) + q);
+            k[1] = v.x;
+            k[2] = v.y;
+            k[3] = v.z;
+            k[4] = v.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) k[1 + j] = i0 + j < n ? __ldg(keys + i0 + j) : kNone;
+        }
+        k[0] = i0 > 0 ? __ldg(keys + i0 - 1) : kNone;
+        k[5] = i0 + 4 < n ? __ldg(keys + i0 + 4) : kNone;
+#pragma unroll
+        for (int j = 1; j <= 4; ++j) {
+            const uint32_t key = k[j];
+            if (key >= ntiles) continue;  // inactive particles, and the slots past n
+            const uint32_t i = uint32_t(i0 + j - 1);
+            if (k[j - 1] != key) tstart[key] = i;
+            if (k[j + 1] != key) tend[key] = i + 1;
+        }
     }
 }
 
@@ -418,7 +442,7 @@ cudaError_t launch_build_items(const uint32_t* sorted_keys, const float* m, int6
     if (e == cudaSuccess) e = cudaMemsetAsync(tend, 0, ntiles * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     if (Pq > 0) {
-        int64_t g = (Pq + 255) / 256;
+        int64_t g = (Pq + 4 * 256 - 1) / (4 * 256);
         if (g > 4096) g = 4096;
         k_tile_ranges<<<int(g), 256, 0, st>>>(sorted_keys, Pq, ntiles, tstart, tend);
     }
