@@ -302,21 +302,23 @@ __device__ __forceinline__ void cols_spectral_lines(const Src& src, float2* s, f
 // complex inverse FFT of Z = X + i Y (X, Y the Hermitian spectra of Fx, Fy,
 // extended to k in [0, N) by X[N-k] = conj X[k]) gives z = fx + i fy directly,
 // the force's own (fx, fy) layout: no half-length pre-split and no
-// interleaving pass.  spec / spec2 / force address one lattice; s holds B
-// padded lines of N points (row b: Phi in [0, M), Psi in [M, N) until Z
-// replaces them) followed by the block_sum scratch (NT/32 * 3B floats);
-// dx: 3B floats of shared scratch.  The y-edge corrections of rows 0, 1,
-// N-2, N-1 follow in apply_edge_rows.
+// interleaving pass.  spec / spec2 / edge / force address one lattice; s
+// holds B padded lines of N points (row b: Phi in [0, M), Psi in [M, N)
+// until Z replaces them) followed by the block_sum scratch (NT/32 * 3B
+// floats); dx: 3B floats of shared scratch.  The y-edge corrections of rows
+// 0, 1, N-2, N-1 enter their Fy spectra from the column pass's edge sums.
 template <int N>
 constexpr size_t c2r_spectral_line() { return size_t(LinePad<N>::value); }
 
 template <int N, int B, int NT>
 __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const float2* __restrict__ spec,
-                                                  const float2* __restrict__ spec2, float4* __restrict__ force,
-                                                  const float2* __restrict__ tw, float g, int y0) {
+                                                  const float2* __restrict__ spec2, const float2* __restrict__ edge,
+                                                  float4* __restrict__ force, const float2* __restrict__ tw, float g,
+                                                  int y0) {
     using C = float2;
     constexpr int M = N / 2;
     constexpr int LP = LinePad<N>::value;
+    const float c12 = g * (1.0f / 12.0f);
     float* red = reinterpret_cast<float*>(s + B * LP);
 #pragma unroll 4  // several transposed loads in flight per thread (measured: -2 us per step at 2048^2)
     for (int idx = threadIdx.x; idx < M * B; idx += NT) {
@@ -353,6 +355,38 @@ __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const fl
             }
         }
     }
+    // y-edge corrections of Fy on rows 0, 1, N-2, N-1, in Fourier space: there
+    // the clamped stencil differs from the periodic one by
+    //   c12 (a01 D01 + a02 D02 + a13 D13)(x),  (a01, a02, a13) = (-8, 1, 0),
+    //   (0, 0, 1), (0, 1, 0), (-8, 0, 1) for y = 0, 1, N-2, N-1,
+    // and the spectra over kx of the y-edge differences D are the column
+    // pass's edge sums (edge[kx * 4 + j], j = D01, D02, D13, with the same
+    // packing of kx = 0 and N/2 in element 0).  The row's inverse FFT is
+    // linear, so adding them to the row's Fy spectrum Psi corrects Fy without
+    // a separate transform of the edge lines.
+    if (y0 <= 1 || y0 + B >= N - 1) {
+        for (int b = 0; b < B; ++b) {
+            const int y = y0 + b;
+            float a01, a02, a13;
+            if (y == 0) {
+                a01 = -8.0f; a02 = 1.0f; a13 = 0.0f;
+            } else if (y == 1) {
+                a01 = 0.0f; a02 = 0.0f; a13 = 1.0f;
+            } else if (y == N - 2) {
+                a01 = 0.0f; a02 = 1.0f; a13 = 0.0f;
+            } else if (y == N - 1) {
+                a01 = -8.0f; a02 = 0.0f; a13 = 1.0f;
+            } else {
+                continue;
+            }
+            for (int k = threadIdx.x; k < M; k += NT) {
+                const C e01 = edge[size_t(k) * 4 + 0], e02 = edge[size_t(k) * 4 + 1], e13 = edge[size_t(k) * 4 + 2];
+                C* p = s + b * LP + pad16(M + k);
+                p->x += c12 * (a01 * e01.x + a02 * e02.x + a13 * e13.x);
+                p->y += c12 * (a01 * e01.y + a02 * e02.y + a13 * e13.y);
+            }
+        }
+    }
     block_sum<NT, 3 * B>(acc, red);  // ends with a barrier: the Fx spectra are complete
     if (threadIdx.x < B) {
         dx[3 * threadIdx.x + 0] = 2.0f * acc[3 * threadIdx.x + 0];
@@ -386,7 +420,6 @@ __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const fl
     }
     __syncthreads();
     // z = fx + i fy, written straight from the last radix stage with the x-edge corrections
-    const float c12 = g * (1.0f / 12.0f);
     float2* frow = reinterpret_cast<float2*>(force) + size_t(y0) * N;
     auto sload = [s](int line, int i) { return s[line * LP + pad16(i)]; };
     auto gstore = [frow, dx, c12](int line, int i, C v) {
@@ -397,19 +430,6 @@ __device__ __forceinline__ void c2r_spectral_rows(float2* s, float* dx, const fl
         frow[size_t(line) * N + i] = v;
     };
     fft_lines<N, B, NT, +1, C, kMaxRadix>(s, sload, gstore, tw, 1);
-}
-
-// y-edge corrections of Fy on rows 0, 1, N-2, N-1 at column x from the three
-// y-edge differences of every column (dy[j * N + x], j = D01, D02, D13); dy /
-// force address one lattice.
-__device__ __forceinline__ void apply_edge_rows(const float* __restrict__ dy, float2* __restrict__ force, int N,
-                                                float g, int x) {
-    const float c12 = g * (1.0f / 12.0f);
-    const float d01 = dy[x], d02 = dy[N + x], d13 = dy[2 * N + x];
-    force[x].y += (-8.0f * d01 + d02) * c12;
-    force[size_t(N) + x].y += d13 * c12;
-    force[size_t(N - 2) * N + x].y += d02 * c12;
-    force[size_t(N - 1) * N + x].y += (d13 - 8.0f * d01) * c12;
 }
 
 }  // namespace cpm

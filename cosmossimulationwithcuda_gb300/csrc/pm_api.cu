@@ -55,8 +55,6 @@ struct cosmos_pm {
     int N = 0, logN = 0, cic = 0, nsm = 0, device = 0;
     int64_t P = 0, Pq = 0, Palloc = 0;
     cudaStream_t stream = nullptr, copy_stream = nullptr;
-    cudaStream_t aux_stream = nullptr;                         // spectral mode: concurrent edge pass
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 
     ParticleArrays buf[2]{};
     int cur = 0;
@@ -70,7 +68,6 @@ struct cosmos_pm {
     float2* force = nullptr;
     float2* spec2 = nullptr;  // spectral mode: y-inverse of the Fy spectrum
     float2* edge = nullptr;   // spectral mode: y-edge differences per line kx
-    float* dy = nullptr;      // spectral mode: y-edge differences per column x
     void* tc_dft = nullptr;   // tensor-core modes: DFT matrix image
     int* tc_status = nullptr; // tensor-core modes: MMA wait timeout flag
     int* wait_status = nullptr;  // step kernels: a bounded copy wait (bulk / tensor-map loads) that ran out
@@ -214,8 +211,8 @@ cudaError_t join_profile_branch(cosmos_pm* h, cudaStream_t st) {
 
 // clear_rho: zero the density behind the row pass (the step clears it for the deposit that follows).
 int launch_spectral(cosmos_pm* h, cudaStream_t st, bool clear_rho = false) {
-    CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->dy, h->kq, h->force, h->tw,
-                                        h->cfg.gravity_multiplier, st, h->aux_stream, h->fork_ev, h->join_ev, 1,
+    CPM_CUDA(cpm::launch_spectral_force(h->N, h->rho, h->spec, h->spec2, h->edge, h->kq, h->force, h->tw,
+                                        h->cfg.gravity_multiplier, st, 1,
                                         is_tc(h->cfg.force_mode) ? &h->tc : nullptr, clear_rho ? h->rho : nullptr,
                                         h->have_maps ? &h->maps : nullptr, h->wait_status, h->cfg.fft_shape));
     return COSMOS_OK;
@@ -433,7 +430,6 @@ void destroy_all(cosmos_pm* h) {
     DeviceGuard g(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
-    if (h->aux_stream) cudaStreamSynchronize(h->aux_stream);
     for (auto& b : h->buf) {
         cudaFree(b.x);
         cudaFree(b.y);
@@ -449,7 +445,6 @@ void destroy_all(cosmos_pm* h) {
     cudaFree(h->force);
     cudaFree(h->spec2);
     cudaFree(h->edge);
-    cudaFree(h->dy);
     cudaFree(h->tc_dft);
     cudaFree(h->tc_status);
     cudaFree(h->wait_status);
@@ -491,9 +486,6 @@ void destroy_all(cosmos_pm* h) {
     if (h->prof_stream) cudaStreamDestroy(h->prof_stream);
     for (auto& t : h->tickets) cudaEventDestroy(t.second);
     for (auto e : h->event_pool) cudaEventDestroy(e);
-    if (h->fork_ev) cudaEventDestroy(h->fork_ev);
-    if (h->join_ev) cudaEventDestroy(h->join_ev);
-    if (h->aux_stream) cudaStreamDestroy(h->aux_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
 }
@@ -622,9 +614,7 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
         return bail(cpm::fail(COSMOS_ERR_CUDA, "initialisation"));
     if (cpm::prepare_conv_passes(N) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "kernel attributes"));
     if (is_spectral(cfg->force_mode)) {
-        if ((rc = dalloc(&h->spec2, NN / 2)) || (rc = dalloc(&h->edge, size_t(N / 2) * 4)) ||
-            (rc = dalloc(&h->dy, size_t(3) * N)))
-            return bail(rc);
+        if ((rc = dalloc(&h->spec2, NN / 2)) || (rc = dalloc(&h->edge, size_t(N / 2) * 4))) return bail(rc);
         if (is_tc(cfg->force_mode)) {
             const int bf16 = cfg->force_mode == COSMOS_FORCE_SPECTRAL_TC_BF16;
             if ((rc = dalloc(reinterpret_cast<unsigned char**>(&h->tc_dft), cpm::tc_dft_bytes(N))) ||
@@ -643,10 +633,6 @@ int create_impl(const cosmos_pm_config* cfg, cosmos_pm** out) {
                 return bail(cpm::fail(COSMOS_ERR_CUDA, std::string("tensor maps: ") + cudaGetErrorString(me)));
             h->have_maps = true;
         }
-        if (cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->join_ev, cudaEventDisableTiming) != cudaSuccess)
-            return bail(cpm::fail(COSMOS_ERR_CUDA, "auxiliary stream"));
     }
     if ((rc = cpm::build_filter(N, h->cic, h->kq, h->tw, h->stream)) != COSMOS_OK) return bail(rc);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(cpm::fail(COSMOS_ERR_CUDA, "create sync"));

@@ -48,7 +48,6 @@ struct EnsClass {
     float2* force = nullptr;
     float2* spec2 = nullptr;
     float2* edge = nullptr;
-    float* dy = nullptr;
     float* kq = nullptr;
     float2* tw = nullptr;
     cpm::RadixScratch rs{};
@@ -59,8 +58,8 @@ struct EnsClass {
     cpm::WorkItem* items = nullptr;
     size_t max_items = 0;
     int item_size = cpm::kItemMax;
-    cudaStream_t stream = nullptr, aux = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, done = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
 };
 
 }  // namespace
@@ -133,13 +132,11 @@ void destroy_class(EnsClass& c) {
     for (auto& b : c.buf)
         for (void* p : {(void*)b.x, (void*)b.y, (void*)b.xo, (void*)b.yo, (void*)b.m, (void*)b.id}) cudaFree(p);
     for (void* p : {(void*)c.off_dev, (void*)c.pos, (void*)c.rho, (void*)c.spec, (void*)c.phi, (void*)c.force,
-                    (void*)c.spec2, (void*)c.edge, (void*)c.dy, (void*)c.kq, (void*)c.tw, (void*)c.rs.keys[0],
+                    (void*)c.spec2, (void*)c.edge, (void*)c.kq, (void*)c.tw, (void*)c.rs.keys[0],
                     (void*)c.rs.keys[1], (void*)c.rs.vals[0], (void*)c.rs.vals[1], (void*)c.rs.counts,
                     (void*)c.tstart, (void*)c.tend, (void*)c.n_items, (void*)c.items, (void*)c.status})
         cudaFree(p);
-    for (cudaEvent_t ev : {c.fork, c.join, c.done})
-        if (ev) cudaEventDestroy(ev);
-    if (c.aux) cudaStreamDestroy(c.aux);
+    if (c.done) cudaEventDestroy(c.done);
     if (c.stream) cudaStreamDestroy(c.stream);
 }
 
@@ -148,7 +145,6 @@ void destroy_all(cosmos_ensemble* e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     for (auto& c : e->classes) {
         if (c.stream) cudaStreamSynchronize(c.stream);
-        if (c.aux) cudaStreamSynchronize(c.aux);
     }
     for (auto& gr : e->graph)
         if (gr) cudaGraphExecDestroy(gr);
@@ -182,16 +178,12 @@ int alloc_class(cosmos_ensemble* e, EnsClass& c) {
         (rc = dalloc(&c.items, c.max_items)) || (rc = dalloc(&c.status, 1)))
         return rc;
     if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
-        if ((rc = dalloc(&c.spec2, S * NN / 2)) || (rc = dalloc(&c.edge, S * size_t(c.N / 2) * 4)) ||
-            (rc = dalloc(&c.dy, S * 3 * size_t(c.N))))
+        if ((rc = dalloc(&c.spec2, S * NN / 2)) || (rc = dalloc(&c.edge, S * size_t(c.N / 2) * 4)))
             return rc;
     } else if ((rc = dalloc(&c.phi, S * NN))) {
         return rc;
     }
     if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming) != cudaSuccess)
         return cpm::fail(COSMOS_ERR_CUDA, "class streams / events");
     cudaStream_t st = e->stream;
@@ -233,8 +225,8 @@ int upload_step_args(cosmos_ensemble* e) {
         x.skip_arrive = e->skip_arrive;
         for (int i = 0; i < x.nclasses; ++i) {
             EnsClass& c = e->classes[i];
-            x.cls[i] = cpm::EnsStepClass{c.N,  c.nsims, c.rho,   c.spec, c.spec2, c.edge,
-                                         c.dy, c.kq,    c.force, c.tw,   c.items, c.n_items, c.buf[parity]};
+            x.cls[i] = cpm::EnsStepClass{c.N,    c.nsims, c.rho, c.spec,  c.spec2,  c.edge,
+                                         c.kq,   c.force, c.tw,  c.items, c.n_items, c.buf[parity]};
         }
     }
     CPM_CUDA(cudaMemcpy(e->pargs, a, sizeof(a), cudaMemcpyHostToDevice));
@@ -360,8 +352,8 @@ int class_body(cosmos_ensemble* e, EnsClass& c) {
     const size_t NN = size_t(c.N) * c.N;
     const float g = e->cfg.gravity_multiplier;
     if (e->cfg.force_mode == COSMOS_FORCE_SPECTRAL) {
-        CPM_CUDA(cpm::launch_spectral_force(c.N, c.rho, c.spec, c.spec2, c.edge, c.dy, c.kq, c.force, c.tw, g, st, c.aux,
-                                            c.fork, c.join, c.nsims, nullptr, nullptr,
+        CPM_CUDA(cpm::launch_spectral_force(c.N, c.rho, c.spec, c.spec2, c.edge, c.kq, c.force, c.tw, g, st, c.nsims,
+                                            nullptr, nullptr,
                                             c.have_maps ? &c.maps : nullptr, c.status));
     } else {
         CPM_CUDA(cpm::launch_conv_passes(c.N, c.rho, c.spec, c.kq, c.phi, c.tw, st, c.nsims));

@@ -3,15 +3,14 @@
 // The graph form of the ensemble step (pm_ensemble.cu) launches every pass of
 // every lattice class as its own kernel node.  Here a single cooperative
 // kernel, one CTA per resident slot, runs the whole step of all classes in
-// five phases separated by grid-wide barriers:
+// four phases separated by grid-wide barriers:
 //   phase 0  row R2C of every density lattice (zeroing each row behind it for
-//            the deposit of phase 4)
+//            the deposit of phase 3)
 //   phase 1  spectral column pass (forward FFT x K, y-edge sums, the two
 //            inverse transforms) of every half-spectrum line block
-//   phase 2  spectral C2R row pass of every row block, and the 3-row C2R of
-//            every lattice's y-edge differences
-//   phase 3  y-edge corrections of the force rows 0, 1, N-2, N-1
-//   phase 4  tile-ordered fused gather + update + deposit of every work item
+//   phase 2  spectral C2R row pass of every row block (the y-edge sums enter
+//            the Fy spectra of rows 0, 1, N-2, N-1)
+//   phase 3  tile-ordered fused gather + update + deposit of every work item
 // A phase's units (row blocks, line blocks, work items) of all classes are
 // numbered consecutively and dealt to the CTAs round-robin.  The bodies are
 // the ones of the per-pass kernels (fft_passes.cuh, tile_step.cuh), so each
@@ -49,7 +48,6 @@ struct EnsShape {
     static constexpr size_t col_smem = 2 * size_t(CB) * LinePad<N>::value * sizeof(float2) + (kEnsThreads / 32) * 6 * 4;
     static constexpr size_t c2r_smem =
         size_t(QB) * LinePad<N>::value * sizeof(float2) + (kEnsThreads / 32) * 3 * QB * 4 + 3 * QB * 4;
-    static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
     static constexpr size_t smem = r2c_smem > col_smem ? (r2c_smem > c2r_smem ? r2c_smem : c2r_smem)
                                                         : (col_smem > c2r_smem ? col_smem : c2r_smem);
 };
@@ -95,9 +93,7 @@ __device__ __forceinline__ int units_r2c(const EnsStepClass& c) { return c.nsims
 template <int N>
 __device__ __forceinline__ int units_col(const EnsStepClass& c) { return c.nsims * ((N / 2) / EnsShape<N>::CB); }
 template <int N>
-__device__ __forceinline__ int units_c2r(const EnsStepClass& c) { return c.nsims * (N / EnsShape<N>::QB + 3); }
-template <int N>
-__device__ __forceinline__ int units_edge(const EnsStepClass& c) { return c.nsims * ((N + kEnsThreads - 1) / kEnsThreads); }
+__device__ __forceinline__ int units_c2r(const EnsStepClass& c) { return c.nsims * (N / EnsShape<N>::QB); }
 
 template <int N>
 __device__ __noinline__ void do_r2c(const EnsStepClass& c, int u, float2* s) {
@@ -128,25 +124,13 @@ __device__ __noinline__ void do_col(const EnsStepClass& c, float g, int u, float
 template <int N>
 __device__ __noinline__ void do_c2r(const EnsStepClass& c, float g, int u, float2* s) {
     using S = EnsShape<N>;
-    constexpr int per = N / S::QB + 3;
+    constexpr int per = N / S::QB;
     const int lat = u / per, r = u - lat * per;
-    if (r < N / S::QB) {  // force rows
-        float* dx = reinterpret_cast<float*>(s + S::QB * LinePad<N>::value) + (kEnsThreads / 32) * 3 * S::QB;
-        const size_t off = size_t(lat) * S::M * N;
-        c2r_spectral_rows<N, S::QB, kEnsThreads>(s, dx, c.spec + off, c.spec2 + off,
-                                                 reinterpret_cast<float4*>(c.force) + off, c.tw, g, r * S::QB);
-    } else {  // y-edge difference row r - N/QB of this lattice
-        c2r_rows<N, 1, kEnsThreads, 4>(s, c.edge + size_t(lat) * S::M * 4, c.dy + size_t(lat) * 3 * N, c.tw,
-                                       r - N / S::QB);
-    }
+    float* dx = reinterpret_cast<float*>(s + S::QB * LinePad<N>::value) + (kEnsThreads / 32) * 3 * S::QB;
+    const size_t off = size_t(lat) * S::M * N;
+    c2r_spectral_rows<N, S::QB, kEnsThreads>(s, dx, c.spec + off, c.spec2 + off, c.edge + size_t(lat) * S::M * 4,
+                                             reinterpret_cast<float4*>(c.force) + off, c.tw, g, r * S::QB);
     __syncthreads();
-}
-
-template <int N>
-__device__ __forceinline__ void do_edge(const EnsStepClass& c, float g, int u) {
-    constexpr int per = (N + kEnsThreads - 1) / kEnsThreads;
-    const int lat = u / per, x = (u - lat * per) * kEnsThreads + int(threadIdx.x);
-    if (x < N) apply_edge_rows(c.dy + size_t(lat) * 3 * N, c.force + size_t(lat) * N * N, N, g, x);
 }
 
 #define CPM_ENS_DISPATCH(N_, CALL) \
@@ -160,7 +144,7 @@ __device__ __forceinline__ void do_edge(const EnsStepClass& c, float g, int u) {
 
 template <int N>
 __device__ __forceinline__ int units_of(const EnsStepClass& c, int phase) {
-    return phase == 0 ? units_r2c<N>(c) : phase == 1 ? units_col<N>(c) : phase == 2 ? units_c2r<N>(c) : units_edge<N>(c);
+    return phase == 0 ? units_r2c<N>(c) : phase == 1 ? units_col<N>(c) : units_c2r<N>(c);
 }
 
 __device__ __forceinline__ int phase_units(const EnsStepClass& c, int phase) {
@@ -176,8 +160,7 @@ __device__ __forceinline__ void run_unit(const EnsStepClass& c, int phase, int u
 #define CPM_R(n_)                                  \
     if (phase == 0) do_r2c<n_>(c, u, s);           \
     else if (phase == 1) do_col<n_>(c, g, u, s);   \
-    else if (phase == 2) do_c2r<n_>(c, g, u, s);   \
-    else do_edge<n_>(c, g, u);
+    else do_c2r<n_>(c, g, u, s);
     CPM_ENS_DISPATCH(c.N, CPM_R)
 #undef CPM_R
 }
@@ -224,11 +207,11 @@ __global__ void __launch_bounds__(kEnsThreads, 2) k_ensemble_step(const EnsStepA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* s = reinterpret_cast<float2*>(smem_raw);
     const EnsStepArgs& a = *args;
-    for (int phase = 0; phase < 4; ++phase) {
+    for (int phase = 0; phase < 3; ++phase) {
         fft_phase(a, phase, s);
         if (!grid_barrier(a.barrier, phase, a.status, a.skip_arrive && phase == 0 && blockIdx.x == 0)) return;
     }
-    fused_phase(a, s);  // phase 4
+    fused_phase(a, s);  // phase 3
 }
 
 }  // namespace

@@ -271,13 +271,14 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, 2 * size_t(B) * LinePad<N>:
     cols_spectral_lines<N, B, NT>(lload, s, spec + size_t(kx0) * N, spec2 + size_t(kx0) * N, edge, kq, tw, g, kx0);
 }
 
-// Rows, spectral force: C2R of Fx and Fy with the x-edge corrections
+// Rows, spectral force: C2R of Fx and Fy with the x- and y-edge corrections
 // (c2r_spectral_rows, fft_passes.cuh).
 template <int N, int B, int NT>
 __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N>::value * sizeof(float2),
                                                  CPM_C2R_SPECTRAL_MINB, (N <= CPM_C2R_FULL_MAX_N ? 64 : 128)>::value))
     k_rows_c2r_spectral(const float2* __restrict__ spec,
                                                              const float2* __restrict__ spec2,
+                                                             const float2* __restrict__ edge,
                                                              float4* __restrict__ force,
                                                              const float2* __restrict__ tw, float g) {
     constexpr int M = N / 2;
@@ -286,16 +287,8 @@ __global__ void __launch_bounds__(NT, (FitBlocks<NT, size_t(B) * LinePad<N>::val
     dependency_wait();
     allow_dependents();
     const size_t lat = size_t(blockIdx.y) * M * N;
-    c2r_spectral_rows<N, B, NT>(reinterpret_cast<float2*>(smem_raw), dx, spec + lat, spec2 + lat, force + lat, tw, g,
-                                int(blockIdx.x) * B);
-}
-
-// y-edge corrections of Fy on rows 0, 1, N-2, N-1 (apply_edge_rows).
-__global__ void k_apply_edge_rows(const float* __restrict__ dy, float2* __restrict__ force, int N, float g) {
-    allow_dependents();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= N) return;
-    apply_edge_rows(dy + size_t(blockIdx.y) * 3 * N, force + size_t(blockIdx.y) * N * N, N, g, x);
+    c2r_spectral_rows<N, B, NT>(reinterpret_cast<float2*>(smem_raw), dx, spec + lat, spec2 + lat,
+                                edge + size_t(blockIdx.y) * M * 4, force + lat, tw, g, int(blockIdx.x) * B);
 }
 
 // ---- filter build helpers ----------------------------------------------------------------
@@ -387,14 +380,8 @@ struct SpecShape {
     // the other column-pass shape (fft_shape = 1): one butterfly per thread from
     // 1024^2 up (twice CS::NT threads), two below (CS::NT threads)
     static constexpr int ACNT = N <= CPM_COLS_FULL_MAX_N ? CS::NT : clamp_threads(2 * CS::B * N / kMaxRadix);
-    static constexpr int ENT0 = M / kMaxRadix;
-    static constexpr int ENT = ENT0 < 64 ? 64 : (ENT0 > 1024 ? 1024 : ENT0);  // edge-row C2R threads
-    static constexpr size_t edge_smem = size_t(LinePad<M>::value) * sizeof(float2);
 };
 
-// The 3-row C2R of the y-edge differences only feeds the 4 boundary rows: it
-// runs on the auxiliary stream, concurrent with the main C2R pass (fork/join
-// with events, which CUDA-graph capture records as graph edges).
 // The tensor-map (TMA) variants of the row and column passes serve lattices
 // from kTmaMinN up (smaller lattices keep per-thread loads: their tiles are a
 // few KB and their landing space would not fit beside the padded lines).
@@ -405,9 +392,8 @@ constexpr int kTmaMinN = 256;
 #endif
 
 template <int N>
-static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                     const float* kq, float2* force, const float2* tw, float g, int batch,
-                                     cudaStream_t st, cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join,
+static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spec2, float2* edge, const float* kq,
+                                     float2* force, const float2* tw, float g, int batch, cudaStream_t st,
                                      const SpectralTc* tc, float* clear, const SpectralMaps* maps, int* status,
                                      int col_shape) {
     using RS = RowShape<float, N>;
@@ -465,17 +451,9 @@ static cudaError_t spectral_passes_n(const float* rho, float2* spec, float2* spe
                                      dim3(CS::NT), SS::col_smem, st, spec, spec2, edge, kq, tw, g)) != cudaSuccess) {
         return e;
     }
-    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(aux, fork, 0)) != cudaSuccess) return e;
-    k_rows_c2r<N, 1, SS::ENT, 4><<<dim3(3, batch), SS::ENT, SS::edge_smem, aux>>>(edge, dy, tw);
-    if ((e = cudaEventRecord(join, aux)) != cudaSuccess) return e;
-    if ((e = launch_dependent(dependent, k_rows_c2r_spectral<N, SS::RB, SS::RNT>, dim3(N / SS::RB, batch),
-                              dim3(SS::RNT), SS::row_smem, st, spec, spec2, reinterpret_cast<float4*>(force), tw,
-                              g)) != cudaSuccess)
-        return e;
-    if ((e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
-    k_apply_edge_rows<<<dim3((N + 255) / 256, batch), 256, 0, st>>>(dy, force, N, g);
-    return cudaGetLastError();
+    return launch_dependent(dependent, k_rows_c2r_spectral<N, SS::RB, SS::RNT>, dim3(N / SS::RB, batch),
+                            dim3(SS::RNT), SS::row_smem, st, spec, spec2, static_cast<const float2*>(edge),
+                            reinterpret_cast<float4*>(force), tw, g);
 }
 
 template <int N>
@@ -498,7 +476,6 @@ static cudaError_t prepare_spectral_n() {
     if ((e = allow_smem(k_cols_spectral<N, CS::B, SS::ACNT>, SS::col_smem_for(SS::ACNT))) != cudaSuccess) return e;
     if ((e = allow_smem(k_cols_spectral<N, CS::B, CS::NT>, SS::col_smem)) != cudaSuccess) return e;
     if ((e = allow_smem(k_cols_spectral<N, CS::B, SS::CNT>, SS::col_smem_for(SS::CNT))) != cudaSuccess) return e;
-    if ((e = allow_smem(k_rows_c2r<N, 1, SS::ENT, 4>, SS::edge_smem)) != cudaSuccess) return e;
     return allow_smem(k_rows_c2r_spectral<N, SS::RB, SS::RNT>, SS::row_smem);
 }
 
@@ -539,9 +516,8 @@ cudaError_t make_spectral_maps(int N, const float* rho, const float2* spec, int 
     }
 }
 
-cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch,
+cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, const float* kq,
+                                  float2* force, const float2* tw, float g, cudaStream_t st, int batch,
                                   const SpectralTc* tc, float* clear, const SpectralMaps* maps, int* status,
                                   int col_shape) {
     if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
@@ -549,8 +525,8 @@ cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2*
     switch (N) {
 #define CPM_CASE(n) \
     case n:         \
-        return spectral_passes_n<n>(rho, spec, spec2, edge, dy, kq, force, tw, g, batch, st, aux, fork, join, tc, \
-                                    clear, maps, status, col_shape);
+        return spectral_passes_n<n>(rho, spec, spec2, edge, kq, force, tw, g, batch, st, tc, clear, maps, status, \
+                                    col_shape);
         CPM_FOR_EACH_N(CPM_CASE)
 #undef CPM_CASE
         default:
@@ -558,7 +534,7 @@ cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2*
     }
 }
 
-int spectral_launches_per_step() { return 5; }
+int spectral_launches_per_step() { return 3; }
 
 template <int N>
 static cudaError_t prepare_conv_n() {

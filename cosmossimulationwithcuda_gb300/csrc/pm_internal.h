@@ -47,13 +47,13 @@ struct SpectralMaps {
 cudaError_t make_spectral_maps(int N, const float* rho, const float2* spec, int batch, SpectralMaps* maps);
 // Test hook of the device allocations: true when this allocation must fail.
 bool alloc_should_fail();
-// aux/fork/join: an auxiliary stream and two events for the concurrent edge pass;
+// edge: the column pass's y-edge sums (N/2 x 4 complex per lattice), which the
+// C2R row pass adds to the Fy spectra of rows 0, 1, N-2, N-1;
 // tc: the tensor-core column pass instead of the FP32 one (nullptr: FP32);
 // maps + status: the row and column passes load their tiles through the
 // tensor maps (from 256^2 up), and a load wait that runs out sets *status.
-cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, float* dy,
-                                  const float* kq, float2* force, const float2* tw, float g, cudaStream_t st,
-                                  cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join, int batch = 1,
+cudaError_t launch_spectral_force(int N, const float* rho, float2* spec, float2* spec2, float2* edge, const float* kq,
+                                  float2* force, const float2* tw, float g, cudaStream_t st, int batch = 1,
                                   const SpectralTc* tc = nullptr, float* clear = nullptr,
                                   const SpectralMaps* maps = nullptr, int* status = nullptr, int col_shape = 0);
 int spectral_launches_per_step();
@@ -165,7 +165,6 @@ struct EnsStepClass {  // one lattice class: nsims lattices of size N stored bac
     int N, nsims;
     float* rho;
     float2 *spec, *spec2, *edge;
-    float* dy;
     const float* kq;
     float2* force;
     const float2* tw;

@@ -132,7 +132,7 @@ def test_ensemble_rejects_bad_configs():
             ens.get_particles(2, 1)       # no simulation 2
         with pytest.raises(_lib.CosmosError):
             ens.get_particles(0, 9)       # beyond P_0
-        assert ens.launches_per_step() == 2 * 6
+        assert ens.launches_per_step() == 2 * 4
 
 
 @pytest.mark.parametrize("persistent", [False, True])

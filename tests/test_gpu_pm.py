@@ -273,7 +273,7 @@ def test_kernel_launch_accounting(cosmos_lib):
     st = ics.uniform(P, N, 0.002, seed=2)
     with _sim(cosmos_lib, N, P, True, dt=0.002, sort_interval=8, force_mode=cosmos_lib.FORCE_SPECTRAL) as s:
         per = s.launches_per_step()
-        assert per == 6  # row R2C, columns, edge C2R, row C2R, edge apply, fused step
+        assert per == 4  # row R2C, columns, row C2R (with the y-edge corrections), fused step
         s.set_state(st)
         k0 = s.kernels_launched()
         s.step(1)  # first-step deposit + sort + step
