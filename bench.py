@@ -587,9 +587,18 @@ def main():
                                             cons1["momentum"][1] - cons0["momentum"][1]) / pscale),
              "note": "FP64 sums on the GPU over active particles; v = (x - xOld)/dt, phi sampled at the NGP cell"}
 
-    # ---- per-stage times (profiled direct launches, events between kernels) ----
+    # ---- per-stage times over the timed region's own steps ----
+    # The fused kernel's time depends on how far the particles drifted since
+    # the last sort, and so on the state's age.  The timed steps are therefore
+    # replayed from the same initial state (same warm-up, same number of
+    # steps) one step per graph launch with CUDA events between the stages,
+    # and each stage's time is averaged over exactly the timed region's steps.
+    sim.set_state(state)
+    conserved()
+    sim.step(args.warmup)
+    sim.synchronize()
     sim.set_profiling(True)
-    prof_steps = 32
+    prof_steps = timed_steps
     names = ["prologue", "fft_conv", "force", "fused_step", "sort"]
     acc = np.zeros(len(names))
     sorts = 0
