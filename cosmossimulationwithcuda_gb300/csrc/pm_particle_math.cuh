@@ -56,6 +56,11 @@ __device__ __forceinline__ float diff4(float ll, float l, float r, float rr, flo
     return __fmul_rn(__fdiv_rn(t, 12.0f), g);
 }
 
+// Vector reduction of two floats into global memory (8-byte aligned address), sm_90+.
+__device__ __forceinline__ void red_add_v2(float* addr, float a, float b) {
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(addr), "f"(a), "f"(b) : "memory");
+}
+
 // Vector reduction into global memory (16-byte aligned address), sm_90+.
 __device__ __forceinline__ void red_add_v4(float* addr, float4 v) {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
